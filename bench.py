@@ -1,0 +1,418 @@
+"""Benchmark of the circuit hot path on GB300.
+
+Default workload (one GPU): the plain circuit at scale -- 64 pieces x 16384
+nodes x 65536 wires per piece (4,194,304 wires), 95% of wires in-piece, 10
+segments per wire, dt = 1e-6, 1000 inner steps, 10 outer loops, fp32, inputs
+from the reference generator's distributions with seed 12345 (inductance
+U[0.001, 0.011)).
+
+One STEP is one whole simulation of that workload, as the reference times it
+(apps/circuit/circuit.cc:164-167, 311-312): the circuit state is reset to its
+generated values, then 10 outer loops of calc_new_currents (all pieces),
+distribute_charge (all pieces), update_voltages (all pieces) run.  The
+metric is wire-segment updates per second = wires x 10 segments x 1000
+inner steps x 10 loops / time.  The working set (411 MB of wire state) is
+larger than L2.
+
+  value  device-resident: state reset by a device copy, kernels on one stream
+  e2e    through the same C-ABI calls with host buffers: every step copies the
+         circuit from pinned host memory to the device, runs the 10 loops and
+         copies the resulting state back
+
+`--impl reference` times the reference's CPU implementation of the same three
+tasks (its shared-low-level execution style: one thread per core, piece p on
+thread p mod T, barriers between launches, 128-byte wires copied by value) on
+the host cores, restated in oracle/ckt_oracle.c because the reference's own
+circuit.cc cannot be built against the runtime it ships with.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--mode fast|exact]
+                       [--impl ours|reference]
+Multi-GPU (torchrun): every rank simulates its own replica of the circuit
+(the path needs no exchange between replicas); value sums all ranks' updates
+over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "wire-segment updates/s at 1 GB300 (plain vs batched/served); p50/p99 solve latency"
+UNIT = "wire-segment updates/s"
+SHAPE = dict(num_pieces=64, nodes_per_piece=16384, wires_per_piece=65536)
+PCT, SEED, INNER_STEPS, OUTER_LOOPS = 95.0, 12345, 1000, 10
+L_OFFSET, L_SCALE = 0.001, 0.01
+FLOPS_PER_WIRE_STEP = 96  # the reference's own count (apps/circuit/circuit.cc:324)
+
+
+def workload_config(mode: str) -> dict:
+    return {
+        "workload": "plain circuit at scale: 64 pieces x 16384 nodes x 65536 wires/piece "
+                    "(4,194,304 wires), 95% in-piece, 10 segments, S=1000 inner steps x "
+                    "10 outer loops per step, seed 12345",
+        "pieces": SHAPE["num_pieces"], "nodes_per_piece": SHAPE["nodes_per_piece"],
+        "wires_per_piece": SHAPE["wires_per_piece"], "inner_steps": INNER_STEPS,
+        "outer_loops_per_step": OUTER_LOOPS, "mode": mode,
+        "l2": "inputs larger than L2 (411 MB of wire state per step)",
+    }
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"ckt_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v == "Active"})
+        loaded = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except ValueError:
+            pass
+    return {}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_sample(threads: int, target_s: float):
+    """A bounded sample of the workload for the CPU implementation: one
+    outer loop of S=1000 over the first `pieces` pieces (whole pieces, one
+    or more per thread), sized to about `target_s` seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ckt_oracle as O
+
+    O.build()
+    p = O.GenParams(SHAPE["num_pieces"], SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"],
+                    PCT, SEED, L_offset=L_OFFSET, L_scale=L_SCALE)
+    base = O.generate(p)
+    # calibrate on one piece per thread at 100 inner steps
+    pieces = min(threads, p.num_pieces)
+    c = base.copy()
+    t = O.baseline_run(c, 1, 100, threads, pieces)
+    per_piece_step = t / 100.0 / math.ceil(pieces / threads)
+    rounds = max(1, min(p.num_pieces // threads if threads <= p.num_pieces else 1,
+                        int(target_s / max(per_piece_step * INNER_STEPS, 1e-9))))
+    pieces = min(p.num_pieces, threads * rounds)
+    return O, p, base, pieces
+
+
+def run_reference_arm(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = cpu_threads()
+    O, p, base, pieces = reference_sample(threads, args.cpu_sample_s)
+    updates = pieces * p.wires_per_piece * 10 * INNER_STEPS
+    for _ in range(args.warmup):
+        O.baseline_run(base.copy(), 1, INNER_STEPS, threads, pieces)
+    times = []
+    for _ in range(args.steps):
+        c = base.copy()
+        times.append(O.baseline_run(c, 1, INNER_STEPS, threads, pieces))
+    total = sum(times)
+    value = updates * args.steps / total
+    sample = (f"1 outer loop x {INNER_STEPS} inner steps over {pieces} of "
+              f"{p.num_pieces} pieces ({pieces * p.wires_per_piece} wires) per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (reference generator, seed 12345)",
+        "config": workload_config("reference CPU tasks (IEEE fp32)"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def fp32_peak(torch, G, stream) -> float:
+    """Measured FP32 FMA throughput (FLOP/s) of this GPU (best of 5)."""
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    sink = torch.zeros(1, device="cuda")
+    blocks, iters = sm * 8, 2048
+    flops = blocks * 256 * iters * 16 * 8 * 2
+    best = 0.0
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(6):
+        s0.record(stream)
+        G.check(G.lib().ckt_fp32_fma_probe(blocks, iters, sink.data_ptr(), stream.cuda_stream))
+        s1.record(stream)
+        s1.synchronize()
+        if i:
+            best = max(best, flops / (s0.elapsed_time(s1) * 1e-3))
+    return best
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--mode", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-sample-s", type=float, default=3.0,
+                    help="target seconds of CPU work per sampled step of the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+
+    import legionorigins_gb300 as G
+    from legionorigins_gb300 import build as B
+    from legionorigins_gb300 import circuit as C
+
+    ws, rank, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    B.build()
+    L = G.lib()
+    mode = G.MODE_FAST if args.mode == "fast" else G.MODE_EXACT
+
+    # CPU baseline first (rank 0, N=1 only), before any GPU work is queued.
+    cpu_baseline = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        O, p, base, pieces = reference_sample(threads, args.cpu_sample_s)
+        t = O.baseline_run(base.copy(), 1, INNER_STEPS, threads, pieces)
+        cpu_baseline = {
+            "value": pieces * p.wires_per_piece * 10 * INNER_STEPS / t, "unit": UNIT,
+            "cores": threads, "kind": "port",
+            "sample": f"1 outer loop x {INNER_STEPS} inner steps over {pieces} of {p.num_pieces} "
+                      f"pieces ({pieces * p.wires_per_piece} wires), reference CPU tasks "
+                      f"restated in C (oracle/ckt_oracle.c), {threads} threads",
+        }
+
+    shape = C.Shape(**SHAPE)
+    host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
+                      SEED + 0, L_OFFSET, L_SCALE)
+    dc = C.DeviceCircuit(host, shape, device=f"cuda:{local}")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    prm = C.params(INNER_STEPS, mode)
+    pristine = {k: dc.t[k].clone() for k in C.STATE_FIELDS}
+    g, w, n = dc.graph.handle, dc.wires(), dc.nodes()
+    E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def reset():
+        with torch.cuda.stream(stream):
+            for k in C.STATE_FIELDS:
+                dc.t[k].copy_(pristine[k], non_blocking=True)
+
+    kernel_events = {"cnc": [], "dc": [], "uv": []}
+
+    def loop(record: bool):
+        for name, fn in (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
+                         ("dc", lambda: L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), sp)),
+                         ("uv", lambda: L.ckt_update_voltages_all(g, n, sp))):
+            if record:
+                a, b = E(), E()
+                a.record(stream)
+                G.check(fn())
+                b.record(stream)
+                kernel_events[name].append((a, b))
+            else:
+                G.check(fn())
+
+    def step(record: bool):
+        reset()
+        for _ in range(OUTER_LOOPS):
+            loop(record)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    barrier()
+    t0, t1 = E(), E()
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    elapsed = t0.elapsed_time(t1) * 1e-3
+    if dist is not None:
+        tt = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    updates_per_step = shape.W * 10 * INNER_STEPS * OUTER_LOOPS
+    value = ws * updates_per_step * args.steps / elapsed
+    launches = sum(len(v) for v in kernel_events.values())
+    kt = {k: [a.elapsed_time(b) * 1e-3 for a, b in v] for k, v in kernel_events.items()}
+
+    # Roofline of the dominant kernel (calc_new_currents, FP32-pipe bound).
+    peak32 = fp32_peak(torch, G, stream)
+    cnc_s = statistics.mean(kt["cnc"])
+    cnc_flops = FLOPS_PER_WIRE_STEP * shape.W * INNER_STEPS
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    hbm_src = "measured (MEASURED_PEAKS.json)" if hbm else "fallback 6800 GB/s"
+    hbm = hbm or 6800.0
+    dc_bytes = 16 * shape.W + 8 * shape.N
+    uv_bytes = 24 * shape.N
+    dc_s, uv_s = statistics.mean(kt["dc"]), statistics.mean(kt["uv"])
+    roofline = {
+        "kernel": "calc_new_currents", "bound": "fp32", "unit": "TFLOP/s",
+        "achieved": cnc_flops / cnc_s / 1e12, "peak": peak32 / 1e12,
+        "frac": cnc_flops / cnc_s / peak32,
+        "peak_source": "measured FP32 FMA throughput (ckt_fp32_fma_probe) on this GPU",
+        "algorithmic": f"{FLOPS_PER_WIRE_STEP} flops per wire-step x {shape.W} wires x "
+                       f"{INNER_STEPS} steps per launch",
+        "traffic": None,
+    }
+    kernels = {
+        "calc_new_currents": {"ms": 1e3 * cnc_s, "tflops": cnc_flops / cnc_s / 1e12,
+                              "frac_fp32_peak": cnc_flops / cnc_s / peak32},
+        "distribute_charge": {"ms": 1e3 * dc_s, "algo_bytes": dc_bytes,
+                              "gbs": dc_bytes / dc_s / 1e9, "frac_hbm": dc_bytes / dc_s / 1e9 / hbm},
+        "update_voltages": {"ms": 1e3 * uv_s, "algo_bytes": uv_bytes,
+                            "gbs": uv_bytes / uv_s / 1e9, "frac_hbm": uv_bytes / uv_s / 1e9 / hbm},
+        "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
+    }
+
+    # End to end through the same C-ABI calls with host buffers.
+    h2d_keys = ("in_ptr", "out_ptr", "in_loc", "out_loc", "L", "R", "C", "current", "voltage",
+                "charge", "node_voltage", "cap", "leak", "locator")
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(host[k])).pin_memory() for k in h2d_keys}
+    out_pinned = {k: torch.empty_like(pinned[k]).pin_memory() for k in C.STATE_FIELDS}
+    h2d = sum(v.numel() * v.element_size() for v in pinned.values())
+    d2h = sum(v.numel() * v.element_size() for v in out_pinned.values())
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for k in h2d_keys:
+                dc.t[k].copy_(pinned[k], non_blocking=True)
+        for _ in range(OUTER_LOOPS):
+            loop(False)
+        with torch.cuda.stream(stream):
+            for k in C.STATE_FIELDS:
+                out_pinned[k].copy_(dc.t[k], non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = E(), E()
+    w0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    barrier()
+    e2e_s = max(e0.elapsed_time(e1) * 1e-3, wall)
+    if dist is not None:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": ws * updates_per_step * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (reference generator distributions, seed 12345)",
+            "config": workload_config(args.mode), "roofline": roofline,
+            "cpu_baseline": cpu_baseline, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "kernels": kernels,
+            "replicas": "one independent circuit per GPU" if ws > 1 else None,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

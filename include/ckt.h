@@ -1,0 +1,241 @@
+/*
+ * ckt.h -- C ABI of the GB300-native circuit hot path.
+ *
+ * Drop-in CUDA variants of the three leaf tasks of LegionOrigins' circuit
+ * simulator (apps/circuit), for sm_103a.  Plain pointers and sizes only: no
+ * CUDA, torch or C++ types cross this boundary (streams are passed as
+ * `void *` holding a cudaStream_t; NULL means the legacy default stream).
+ *
+ * Data contract (apps/circuit/circuit.h:13-76):
+ *   - node and wire "pointers" are 32-bit absolute indices into their
+ *     regions (runtime/common.h:11-52, apps/circuit/circuit.h:46-47);
+ *   - a piece owns the contiguous wire range [first_wire, first_wire +
+ *     num_wires) and node range [first_node, first_node + num_nodes)
+ *     (apps/circuit/circuit.cc:1270-1280);
+ *   - region instances are structure-of-arrays views indexed by absolute
+ *     index, the role GPU_Accessor's array_base plays in the reference
+ *     (runtime/lowlevel.h:749-833); per-segment wire arrays are
+ *     segment-major with a caller-given stride;
+ *   - each wire has CKT_SEGMENTS = 10 segments (circuit.h:42).
+ *
+ * Every entry point returns a ckt_status; none asserts, traps or exits.
+ * ckt_last_error() describes the last failure on the calling thread.
+ */
+#ifndef CKT_H
+#define CKT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CKT_SEGMENTS 10
+#define CKT_ABI_VERSION 1
+
+typedef enum {
+  CKT_OK = 0,
+  CKT_EINVAL = 1,    /* bad argument */
+  CKT_ECUDA = 2,     /* a CUDA call failed */
+  CKT_EBOUNDS = 3,   /* a pointer or location failed validation */
+  CKT_ETIMEOUT = 4,  /* a bounded device wait ran out */
+  CKT_ENOMEM = 5,    /* allocation refused (budget or device) */
+  CKT_EBUSY = 6,     /* no free slot / queue full */
+  CKT_ECANCELLED = 7 /* request cancelled */
+} ckt_status;
+
+/* PointerLocation (apps/circuit/circuit.h:12-16). */
+typedef enum { CKT_PRIVATE_PTR = 0, CKT_SHARED_PTR = 1, CKT_GHOST_PTR = 2 } ckt_pointer_location;
+
+/* Arithmetic of calc_new_currents. */
+typedef enum {
+  /* IEEE fp32 exactly as the reference writes it (correctly rounded
+   * divides, no contraction): bit-identical to the reference CPU task. */
+  CKT_MODE_EXACT = 0,
+  /* Loop-invariant quotients L/dt, 1/R and dt/C hoisted out of the inner
+   * loop and fused multiply-adds: within 1e-5 relative of EXACT. */
+  CKT_MODE_FAST = 1
+} ckt_mode;
+
+/* Wire initialisation of calc_new_currents. */
+typedef enum {
+  /* GPU task semantics (apps/circuit/circuit_gpu.cu:107-112): new_v[0] =
+   * in-node voltage, new_v[i+1] = wire.voltage[i]. */
+  CKT_INIT_KERNEL = 0,
+  /* CPU task semantics (apps/circuit/circuit.cc:380-384): new_v[i] =
+   * wire.voltage[i] for i < 9, new_v[9] read before written (defined here
+   * as 0), in-node voltage unused. */
+  CKT_INIT_CPU_TASK = 1
+} ckt_init;
+
+/* CircuitPiece (apps/circuit/circuit.h:62-69) minus its region handles. */
+typedef struct {
+  uint32_t first_wire;
+  uint32_t num_wires;
+  uint32_t first_node;
+  uint32_t num_nodes;
+} ckt_piece;
+
+/* Wire region instance (CircuitWire, apps/circuit/circuit.h:46-54), SoA.
+ * current[k*seg_stride + w] is segment k of wire w (k < 10); voltage has 9
+ * segments.  All pointers are device pointers. */
+typedef struct {
+  const uint32_t *in_ptr;
+  const uint32_t *out_ptr;
+  const uint8_t *in_loc;
+  const uint8_t *out_loc;
+  const float *inductance;
+  const float *resistance;
+  const float *capacitance;
+  float *current;
+  float *voltage;
+  int64_t seg_stride;
+} ckt_wires;
+
+/* Node region instance (CircuitNode, apps/circuit/circuit.h:35-40), SoA,
+ * absolute node index.  Device pointers. */
+typedef struct {
+  float *charge;
+  float *voltage;
+  const float *capacitance;
+  const float *leakage;
+} ckt_nodes;
+
+typedef struct {
+  int32_t steps; /* inner steps (STEPS, circuit.h:43; a runtime value here) */
+  float dt;      /* DELTAT (circuit.h:44) = (float)1e-6 */
+  int32_t mode;  /* ckt_mode */
+  int32_t init;  /* ckt_init */
+} ckt_params;
+
+/* Static contribution graph of one circuit: for every node, the wire ends
+ * that deposit charge on it, in the reference's reduction order.  Built once
+ * from the wire endpoints (the role the runtime's region tree and reduction
+ * instances play in the reference). */
+typedef struct ckt_graph ckt_graph;
+
+/* ------------------------------------------------------------------------
+ * Library
+ * ---------------------------------------------------------------------- */
+int ckt_abi_version(void);
+const char *ckt_last_error(void);
+const char *ckt_status_string(int status);
+/* Default parameters: steps 10000, dt (float)1e-6, EXACT, KERNEL init. */
+void ckt_default_params(ckt_params *out);
+
+/* ------------------------------------------------------------------------
+ * The three leaf tasks, per piece (drop-in for the reference's GPU task
+ * bodies).  Asynchronous on `stream`.
+ * ---------------------------------------------------------------------- */
+
+/* Replaces calc_new_currents_gpu (apps/circuit/circuit.h:83-88,
+ * apps/circuit/circuit_gpu.cu:186-205).  Reads in/out node voltages from
+ * pvt, shr or ghost by the wire's location (circuit_gpu.cu:40-59); writes
+ * current[10] and voltage[9] of every wire of the piece. */
+int ckt_calc_new_currents(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                          ckt_nodes shr, ckt_nodes ghost, const ckt_params *prm,
+                          void *stream);
+
+/* Replaces distribute_charge_gpu (apps/circuit/circuit.h:90-95,
+ * apps/circuit/circuit_gpu.cu:245-304).  Deposits -dt*I[0] on the in-node
+ * and +dt*I[9] on the out-node of each wire of piece `piece_index` of
+ * `graph`: private nodes' charge is updated in place in wire order
+ * (apply<true>); shared and ghost nodes fold into `shr_fold` / `ghost_fold`
+ * (float per absolute node index, the reduction instances of
+ * runtime/lowlevel.h:835-881) in wire order.  Deterministic: no atomics. */
+int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires wires,
+                          ckt_nodes pvt, float *shr_fold, float *ghost_fold,
+                          const ckt_params *prm, void *stream);
+
+/* The runtime's application of piece `piece_index`'s reduction instances
+ * (runtime/lowlevel_dma.cc:323-355): charge[x] += fold[x] for every shared
+ * or ghost node the piece touched, then fold[x] = 0.  Call pieces in
+ * ascending order to reproduce the reference's canonical reduction. */
+int ckt_apply_fold(const ckt_graph *graph, int32_t piece_index, float *shr_fold,
+                   float *ghost_fold, float *charge, void *stream);
+
+/* Replaces update_voltages_gpu (apps/circuit/circuit.h:97-101,
+ * apps/circuit/circuit_gpu.cu:306-368): for every node of the piece,
+ * choose pvt or shr by locator[x] (1 private, 0 shared), then
+ * v += q/C; v *= (1 - leak); q = 0. */
+int ckt_update_voltages(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
+                        const int32_t *locator, void *stream);
+
+/* Replaces sanity_check_wires_gpu (apps/circuit/circuit.h:103-104,
+ * apps/circuit/circuit_gpu.cu:151-217) without its asserts: validates every
+ * wire of the piece (locations in range, in-node inside the piece,
+ * private/shared out-node inside the piece, ghost out-node outside it and
+ * below num_nodes_total).  Synchronises `stream`; returns CKT_EBOUNDS and
+ * stores the first bad wire in *first_bad (or -1) when a check fails. */
+int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num_nodes_total,
+                           int64_t *first_bad, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Index-space launches: one launch per task over all pieces of a circuit
+ * (the three execute_index_space calls of apps/circuit/circuit.cc:250-298),
+ * bit-identical to running the per-piece calls in piece order followed by
+ * ckt_apply_fold in piece order.
+ * ---------------------------------------------------------------------- */
+int ckt_calc_new_currents_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream);
+int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream);
+int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Contribution graph
+ * ---------------------------------------------------------------------- */
+
+/* Builds the graph from HOST copies of the wire endpoints.  pieces[] must
+ * tile [0, W) with ascending first_wire; num_nodes is the node region size.
+ * Validates every pointer and location (CKT_EBOUNDS names the first bad
+ * wire in ckt_last_error()).  Allocates device memory. */
+int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
+                     const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
+                     const uint8_t *out_loc, ckt_graph **out);
+int ckt_graph_destroy(ckt_graph *graph);
+/* Sizes: wires, nodes, pieces, and device bytes held. */
+int ckt_graph_info(const ckt_graph *graph, int64_t *num_wires, int64_t *num_nodes,
+                   int32_t *num_pieces, int64_t *device_bytes);
+
+/* ------------------------------------------------------------------------
+ * Generator: restatement of load_circuit (apps/circuit/circuit.cc:1071-1288)
+ * producing the same drand48 stream, graph and initial values.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t num_pieces;      /* -p   */
+  int32_t nodes_per_piece; /* -npp */
+  int32_t wires_per_piece; /* -wpp */
+  int32_t reserved;
+  double pct_wire_in_piece; /* -pct, compared as (100*drand48()) < pct */
+  int64_t random_seed;      /* -s   */
+  double L_offset;          /* inductance = drand48()*L_scale + L_offset; */
+  double L_scale;           /* the reference hard-codes 0.01 and 0.1     */
+} ckt_gen_params;
+
+/* Host structure-of-arrays circuit (caller-allocated; W = P*wpp, N = P*npp).
+ * current is [10][W], voltage [9][W]. */
+typedef struct {
+  uint32_t *in_ptr, *out_ptr;
+  uint8_t *in_loc, *out_loc;
+  float *inductance, *resistance, *capacitance;
+  float *current, *voltage;
+  float *charge, *node_voltage, *node_capacitance, *node_leakage;
+  int32_t *locator;
+} ckt_host_circuit;
+
+int ckt_generate(const ckt_gen_params *p, ckt_host_circuit *out);
+
+/* ------------------------------------------------------------------------
+ * Measurement helper (no counterpart in the reference): FP32 FMA throughput
+ * probe.  Launches `blocks` x 256 threads, each issuing iters*16*8
+ * independent fused multiply-adds (2 flops each); time it on `stream` to
+ * get the device's FP32-pipe peak.  `sink` is a device float it may write.
+ * ---------------------------------------------------------------------- */
+int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, float *sink, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CKT_H */

@@ -1,0 +1,128 @@
+"""GB300-native circuit hot path (calc_new_currents / distribute_charge /
+update_voltages of LegionOrigins' circuit simulator) behind a C ABI.
+
+The compute lives in legionorigins_gb300/_build/libckt.so (CUDA for sm_103a
+plus host C++), built by legionorigins_gb300.build.build().  This module
+is the ctypes binding of include/ckt.h.  There is no CPU fallback: if the
+library is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+__all__ = ["lib", "CktError", "Piece", "Wires", "Nodes", "Params", "GenParams", "HostCircuit",
+           "MODE_EXACT", "MODE_FAST", "INIT_KERNEL", "INIT_CPU_TASK", "check"]
+
+LIB_PATH = _build.LIB
+
+MODE_EXACT, MODE_FAST = 0, 1
+INIT_KERNEL, INIT_CPU_TASK = 0, 1
+PRIVATE_PTR, SHARED_PTR, GHOST_PTR = 0, 1, 2
+SEGMENTS = 10
+DT = float.fromhex("0x1.0c6f7ap-20")  # (float)1e-6
+
+
+class CktError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ckt status {status}: {msg}")
+        self.status = status
+
+
+class Piece(ctypes.Structure):
+    _fields_ = [("first_wire", ctypes.c_uint32), ("num_wires", ctypes.c_uint32),
+                ("first_node", ctypes.c_uint32), ("num_nodes", ctypes.c_uint32)]
+
+
+class Wires(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("in_ptr", "out_ptr", "in_loc", "out_loc",
+                                              "inductance", "resistance", "capacitance",
+                                              "current", "voltage")] + [
+        ("seg_stride", ctypes.c_int64)]
+
+
+class Nodes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("charge", "voltage", "capacitance", "leakage")]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int32), ("dt", ctypes.c_float), ("mode", ctypes.c_int32),
+                ("init", ctypes.c_int32)]
+
+
+class GenParams(ctypes.Structure):
+    _fields_ = [("num_pieces", ctypes.c_int32), ("nodes_per_piece", ctypes.c_int32),
+                ("wires_per_piece", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("pct_wire_in_piece", ctypes.c_double), ("random_seed", ctypes.c_int64),
+                ("L_offset", ctypes.c_double), ("L_scale", ctypes.c_double)]
+
+
+class HostCircuit(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "in_ptr", "out_ptr", "in_loc", "out_loc", "inductance", "resistance", "capacitance",
+        "current", "voltage", "charge", "node_voltage", "node_capacitance", "node_leakage",
+        "locator")]
+
+
+# (name, restype, argtypes) of every exported symbol declared in include/ckt.h
+_P = ctypes.c_void_p
+_I32, _I64, _U32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32
+SIGNATURES = {
+    "ckt_abi_version": (ctypes.c_int, []),
+    "ckt_last_error": (ctypes.c_char_p, []),
+    "ckt_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "ckt_default_params": (None, [ctypes.POINTER(Params)]),
+    "ckt_calc_new_currents": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, Nodes, Nodes, Nodes,
+                                             ctypes.POINTER(Params), _P]),
+    "ckt_distribute_charge": (ctypes.c_int, [_P, _I32, Wires, Nodes, _P, _P,
+                                             ctypes.POINTER(Params), _P]),
+    "ckt_apply_fold": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P]),
+    "ckt_update_voltages": (ctypes.c_int, [ctypes.POINTER(Piece), Nodes, Nodes, _P, _P]),
+    "ckt_sanity_check_wires": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, _U32,
+                                              ctypes.POINTER(_I64), _P]),
+    "ckt_calc_new_currents_all": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _P]),
+    "ckt_distribute_charge_all": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _P]),
+    "ckt_update_voltages_all": (ctypes.c_int, [_P, Nodes, _P]),
+    "ckt_graph_create": (ctypes.c_int, [ctypes.POINTER(Piece), _I32, _U32, _P, _P, _P, _P,
+                                        ctypes.POINTER(_P)]),
+    "ckt_graph_destroy": (ctypes.c_int, [_P]),
+    "ckt_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                                      ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
+    "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
+    "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _P, _P]),
+}
+
+_lib = None
+
+
+def lib(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load libckt.so.  Raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built; run legionorigins_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != 0:
+        msg = lib().ckt_last_error().decode(errors="replace")
+        raise CktError(status, msg)
+
+
+def default_params(steps: int = 10000, mode: int = MODE_EXACT, init: int = INIT_KERNEL) -> Params:
+    p = Params()
+    lib().ckt_default_params(ctypes.byref(p))
+    p.steps, p.mode, p.init = steps, mode, init
+    return p

@@ -1,0 +1,200 @@
+// ckt_graph.cpp -- builds the static contribution graph of a circuit on the
+// host and uploads it.
+//
+// The graph fixes the order in which distribute_charge's contributions are
+// summed so that the GPU reproduces one legal schedule of the reference's
+// reduction bit for bit:
+//   * private nodes (apps/circuit/circuit.cc:184-196: READ_WRITE, EXCLUSIVE)
+//     receive their contributions in place, in wire order (reduce() on a
+//     normal instance is apply<true>, runtime/lowlevel.h:484-489);
+//   * shared and ghost nodes (REDUCE, SIMULTANEOUS) receive, per piece, the
+//     fold of that piece's contributions in wire order starting from the
+//     identity 0.0f (runtime/lowlevel.h:478-483, circuit.cc:30); the runtime
+//     then applies each piece's fold instance to the node
+//     (runtime/lowlevel_dma.cc:323-355); pieces are applied in ascending
+//     order here.
+#include <algorithm>
+#include <cstring>
+
+#include "ckt_internal.h"
+
+namespace ckt {
+
+template <typename T>
+static int upload(T **dst, const std::vector<T> &src, int64_t *bytes) {
+  const size_t n = std::max<size_t>(src.size(), 1);
+  CKT_CUDA(cudaMalloc(reinterpret_cast<void **>(dst), n * sizeof(T)));
+  *bytes += (int64_t)(n * sizeof(T));
+  if (!src.empty())
+    CKT_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return CKT_OK;
+}
+
+static void free_graph(ckt_graph *g) {
+  if (!g) return;
+  cudaFree(g->node_off);
+  cudaFree(g->node_ent);
+  cudaFree(g->touch_node);
+  cudaFree(g->touch_loc);
+  cudaFree(g->touch_off);
+  cudaFree(g->piece_ent);
+  delete g;
+}
+
+}  // namespace ckt
+
+using namespace ckt;
+
+extern "C" {
+
+int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
+                     const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
+                     const uint8_t *out_loc, ckt_graph **out) {
+  CKT_REQUIRE(out != nullptr, "out is NULL");
+  *out = nullptr;
+  CKT_REQUIRE(num_pieces >= 1 && pieces != nullptr, "need at least one piece");
+  // Pieces tile [0, W) in order; node ranges lie inside [0, N) and are disjoint.
+  int64_t W = 0;
+  std::vector<int32_t> node_owner(num_nodes, -1);
+  for (int32_t k = 0; k < num_pieces; k++) {
+    const ckt_piece &p = pieces[k];
+    CKT_REQUIRE(p.first_wire == (uint64_t)W, "piece %d starts at wire %u, expected %lld", k,
+                p.first_wire, (long long)W);
+    W += p.num_wires;
+    CKT_REQUIRE((uint64_t)p.first_node + p.num_nodes <= num_nodes,
+                "piece %d node range [%u, %llu) exceeds %u nodes", k, p.first_node,
+                (unsigned long long)p.first_node + p.num_nodes, num_nodes);
+    for (uint32_t i = 0; i < p.num_nodes; i++) {
+      CKT_REQUIRE(node_owner[p.first_node + i] < 0, "node %u belongs to pieces %d and %d",
+                  p.first_node + i, node_owner[p.first_node + i], k);
+      node_owner[p.first_node + i] = k;
+    }
+  }
+  CKT_REQUIRE(W <= kMaxWires, "%lld wires exceed the limit %lld", (long long)W,
+              (long long)kMaxWires);
+  CKT_REQUIRE(W == 0 || (in_ptr && out_ptr && in_loc && out_loc), "wire arrays are NULL");
+  const int64_t N = num_nodes;
+
+  // Validate every endpoint (sanity_check_positions, circuit_gpu.cu:151-184)
+  // and that no node is used both as private and as shared/ghost.
+  std::vector<uint8_t> kind(N, 0);  // 0 unused, 1 private, 2 shared/ghost
+  for (int32_t k = 0; k < num_pieces; k++) {
+    const ckt_piece &p = pieces[k];
+    for (int64_t w = p.first_wire; w < (int64_t)p.first_wire + p.num_wires; w++) {
+      const uint32_t xs[2] = {in_ptr[w], out_ptr[w]};
+      const uint8_t ls[2] = {in_loc[w], out_loc[w]};
+      for (int e = 0; e < 2; e++) {
+        const uint32_t x = xs[e];
+        if ((int64_t)x >= N || ls[e] > CKT_GHOST_PTR)
+          return set_error(CKT_EBOUNDS, "wire %lld: %s pointer %u / location %u out of range",
+                           (long long)w, e ? "out" : "in", x, ls[e]);
+        const bool inside = node_owner[x] == k;
+        const bool ok = (e == 0) ? (inside && ls[e] != CKT_GHOST_PTR)
+                                 : (inside ? ls[e] != CKT_GHOST_PTR : ls[e] == CKT_GHOST_PTR);
+        if (!ok)
+          return set_error(CKT_EBOUNDS, "wire %lld: %s pointer %u inconsistent with location %u",
+                           (long long)w, e ? "out" : "in", x, ls[e]);
+        const uint8_t kd = ls[e] == CKT_PRIVATE_PTR ? 1 : 2;
+        if (kind[x] && kind[x] != kd)
+          return set_error(CKT_EBOUNDS,
+                           "wire %lld: node %u is referenced both as private and as shared",
+                           (long long)w, x);
+        kind[x] = kd;
+      }
+    }
+  }
+
+  ckt_graph *g = new ckt_graph();
+  g->W = W;
+  g->N = N;
+  g->P = num_pieces;
+  g->pieces.assign(pieces, pieces + num_pieces);
+
+  // Whole-circuit CSR: counting sort of the 2W endpoints by node; filling in
+  // wire order keeps (wire, end) order inside each node.
+  std::vector<uint32_t> off(N + 1, 0), ent(2 * W);
+  for (int64_t w = 0; w < W; w++) {
+    off[in_ptr[w] + 1]++;
+    off[out_ptr[w] + 1]++;
+  }
+  for (int64_t x = 0; x < N; x++) off[x + 1] += off[x];
+  {
+    std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+    std::vector<int32_t> last_piece(N, -1);
+    for (int32_t k = 0; k < num_pieces; k++) {
+      const ckt_piece &p = pieces[k];
+      for (int64_t w = p.first_wire; w < (int64_t)p.first_wire + p.num_wires; w++) {
+        const uint32_t xs[2] = {in_ptr[w], out_ptr[w]};
+        for (uint32_t e = 0; e < 2; e++) {
+          const uint32_t x = xs[e];
+          const uint32_t start = last_piece[x] != k ? 1u : 0u;
+          last_piece[x] = k;
+          ent[fill[x]++] = ((uint32_t)w << 2) | (e << 1) | start;
+        }
+      }
+    }
+  }
+  for (int64_t x = 0; x < N; x++)
+    if (kind[x] != 2) off[x] |= kPrivateBit;
+
+  // Per-piece CSR over touched nodes, nodes ascending, wire order inside.
+  std::vector<uint32_t> touch_node, touch_off, pent;
+  std::vector<uint8_t> touch_loc;
+  g->touch_first.assign(num_pieces + 1, 0);
+  pent.reserve(2 * W);
+  std::vector<uint64_t> keys;
+  for (int32_t k = 0; k < num_pieces; k++) {
+    const ckt_piece &p = pieces[k];
+    g->touch_first[k] = (int64_t)touch_node.size();
+    keys.clear();
+    for (uint32_t i = 0; i < p.num_wires; i++) {
+      const int64_t w = (int64_t)p.first_wire + i;
+      keys.push_back(((uint64_t)in_ptr[w] << 32) | (2u * i));
+      keys.push_back(((uint64_t)out_ptr[w] << 32) | (2u * i + 1));
+    }
+    std::sort(keys.begin(), keys.end());
+    for (size_t j = 0; j < keys.size(); j++) {
+      const uint32_t x = (uint32_t)(keys[j] >> 32);
+      const uint32_t local = (uint32_t)keys[j];
+      const uint32_t w = p.first_wire + (local >> 1), e = local & 1u;
+      if (j == 0 || (uint32_t)(keys[j - 1] >> 32) != x) {
+        touch_node.push_back(x);
+        touch_loc.push_back(e ? out_loc[w] : in_loc[w]);
+        touch_off.push_back((uint32_t)pent.size());
+      }
+      pent.push_back((w << 1) | e);
+    }
+  }
+  g->touch_first[num_pieces] = (int64_t)touch_node.size();
+  touch_off.push_back((uint32_t)pent.size());
+
+  int rc = CKT_OK;
+  if ((rc = upload(&g->node_off, off, &g->device_bytes)) ||
+      (rc = upload(&g->node_ent, ent, &g->device_bytes)) ||
+      (rc = upload(&g->touch_node, touch_node, &g->device_bytes)) ||
+      (rc = upload(&g->touch_loc, touch_loc, &g->device_bytes)) ||
+      (rc = upload(&g->touch_off, touch_off, &g->device_bytes)) ||
+      (rc = upload(&g->piece_ent, pent, &g->device_bytes))) {
+    free_graph(g);
+    return rc;
+  }
+  *out = g;
+  return CKT_OK;
+}
+
+int ckt_graph_destroy(ckt_graph *graph) {
+  free_graph(graph);
+  return CKT_OK;
+}
+
+int ckt_graph_info(const ckt_graph *g, int64_t *num_wires, int64_t *num_nodes,
+                   int32_t *num_pieces, int64_t *device_bytes) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  if (num_wires) *num_wires = g->W;
+  if (num_nodes) *num_nodes = g->N;
+  if (num_pieces) *num_pieces = g->P;
+  if (device_bytes) *device_bytes = g->device_bytes;
+  return CKT_OK;
+}
+
+}  // extern "C"

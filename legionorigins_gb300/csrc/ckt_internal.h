@@ -1,0 +1,73 @@
+// ckt_internal.h -- shared helpers of the circuit library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ckt.h"
+
+namespace ckt {
+
+// Records the failure message for ckt_last_error() and returns `status`.
+int set_error(int status, const char *fmt, ...);
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+#define CKT_CUDA(expr)                                                          \
+  do {                                                                          \
+    cudaError_t ckt_err_ = (expr);                                              \
+    if (ckt_err_ != cudaSuccess)                                                \
+      return ::ckt::set_error(CKT_ECUDA, "%s failed: %s (%s:%d)", #expr,        \
+                              cudaGetErrorString(ckt_err_), __FILE__, __LINE__); \
+  } while (0)
+
+#define CKT_CHECK_LAUNCH()                                                      \
+  do {                                                                          \
+    cudaError_t ckt_err_ = cudaGetLastError();                                  \
+    if (ckt_err_ != cudaSuccess)                                                \
+      return ::ckt::set_error(CKT_ECUDA, "kernel launch failed: %s (%s:%d)",    \
+                              cudaGetErrorString(ckt_err_), __FILE__, __LINE__); \
+  } while (0)
+
+#define CKT_REQUIRE(cond, ...)                                                  \
+  do {                                                                          \
+    if (!(cond)) return ::ckt::set_error(CKT_EINVAL, __VA_ARGS__);              \
+  } while (0)
+
+// Entry encodings of the contribution graph.
+//   node CSR entry: (wire << 2) | (end << 1) | starts_new_piece_group
+//   piece CSR entry: (wire << 1) | end          (end: 0 = in, 1 = out)
+//   node offset word: offset | (node_is_private << 31)
+constexpr uint32_t kPrivateBit = 0x80000000u;
+constexpr uint32_t kOffsetMask = 0x7fffffffu;
+constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 31 bits
+
+int validate_wires(const ckt_wires &w);
+int validate_nodes(const ckt_nodes &n, const char *what);
+int validate_params(const ckt_params *p);
+
+}  // namespace ckt
+
+// The graph object behind the opaque ckt_graph handle.
+struct ckt_graph {
+  int64_t W = 0, N = 0;
+  int32_t P = 0;
+  std::vector<ckt_piece> pieces;
+  // Whole-circuit node CSR (device).
+  uint32_t *node_off = nullptr;  // [N + 1]
+  uint32_t *node_ent = nullptr;  // [2W]
+  // Per-piece CSR over the nodes each piece touches (device), concatenated
+  // in piece order; piece k owns touched slots [touch_first[k],
+  // touch_first[k+1]).
+  std::vector<int64_t> touch_first;  // host, [P + 1]
+  uint32_t *touch_node = nullptr;    // [T]
+  uint8_t *touch_loc = nullptr;      // [T]
+  uint32_t *touch_off = nullptr;     // [T + 1] into piece_ent
+  uint32_t *piece_ent = nullptr;     // [2W]
+  int64_t device_bytes = 0;
+};

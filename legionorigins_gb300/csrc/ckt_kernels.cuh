@@ -1,0 +1,283 @@
+// ckt_kernels.cuh -- sm_103a kernels of the circuit hot path.
+//
+// Arithmetic follows the reference task bodies operation by operation
+// (apps/circuit/circuit_gpu.cu:114-129, 281-283, 330-345; the CPU tasks at
+// apps/circuit/circuit.cc:386-401, 430-431, 1300-1302).  Every operation of
+// the EXACT paths uses an explicitly rounded intrinsic so that no multiply
+// is ever contracted into an add: results are bit-identical to the
+// reference's IEEE fp32 arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ckt.h"
+
+namespace ckt {
+
+// ---------------------------------------------------------------------------
+// calc_new_currents: one thread per wire.  The 10 segment currents and 11
+// node/segment voltages of a wire live in registers across the whole inner
+// time-step loop; wire fields are structure-of-arrays so a warp's loads and
+// stores of any one field are one contiguous 128-byte line.
+// ---------------------------------------------------------------------------
+template <int MODE>
+struct WireStep;
+
+// EXACT: ((dv) - (L*(i-I0))/dt) / R and V0 + (dt*(i_k - i_k+1))/C, each
+// operation rounded exactly as the reference's fp32 source.
+template <>
+struct WireStep<CKT_MODE_EXACT> {
+  float L, R, C, dt;
+  __device__ __forceinline__ WireStep(float l, float r, float c, float d) : L(l), R(r), C(c), dt(d) {}
+  __device__ __forceinline__ void step(float (&ni)[10], float (&nv)[11], const float (&I0)[10],
+                                       const float (&V0)[9]) const {
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      const float dv = __fsub_rn(nv[k + 1], nv[k]);
+      const float q = __fdiv_rn(__fmul_rn(L, __fsub_rn(ni[k], I0[k])), dt);
+      ni[k] = __fdiv_rn(__fsub_rn(dv, q), R);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(__fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1])), C));
+  }
+};
+
+// FAST: the three divisors are loop-invariant, so their quotients are
+// computed once per wire (correctly rounded) and every inner-loop divide
+// becomes a multiply; the subtract-then-scale pairs become FMAs.
+// 4 FP32 instructions per current, 2 per voltage = 58 per wire-step.
+template <>
+struct WireStep<CKT_MODE_FAST> {
+  float nLdt, rR, dtC;
+  __device__ __forceinline__ WireStep(float l, float r, float c, float d) {
+    nLdt = -__fdiv_rn(l, d);
+    rR = __fdiv_rn(1.0f, r);
+    dtC = __fdiv_rn(d, c);
+  }
+  __device__ __forceinline__ void step(float (&ni)[10], float (&nv)[11], const float (&I0)[10],
+                                       const float (&V0)[9]) const {
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      const float dv = __fsub_rn(nv[k + 1], nv[k]);
+      ni[k] = __fmul_rn(__fmaf_rn(nLdt, __fsub_rn(ni[k], I0[k]), dv), rR);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k + 1] = __fmaf_rn(dtC, __fsub_rn(ni[k], ni[k + 1]), V0[k]);
+  }
+};
+
+__device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *pvt,
+                                                      const float *shr, const float *ghost) {
+  // get_node (apps/circuit/circuit_gpu.cu:40-59) without its assert: a
+  // location outside {0,1,2} reads the ghost instance; ckt_sanity_check_wires
+  // and ckt_graph_create reject such wires.
+  return loc == CKT_PRIVATE_PTR ? pvt : (loc == CKT_SHARED_PTR ? shr : ghost);
+}
+
+template <int MODE, int INIT>
+__global__ void __launch_bounds__(256)
+    cnc_kernel(uint32_t first_wire, uint32_t num_wires, const uint32_t *__restrict__ in_ptr,
+               const uint32_t *__restrict__ out_ptr, const uint8_t *__restrict__ in_loc,
+               const uint8_t *__restrict__ out_loc, const float *__restrict__ Lw,
+               const float *__restrict__ Rw, const float *__restrict__ Cw,
+               float *__restrict__ cur, float *__restrict__ vol, int64_t S,
+               const float *__restrict__ v_pvt, const float *__restrict__ v_shr,
+               const float *__restrict__ v_ghost, int steps, float dt) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= num_wires) return;
+  const int64_t w = (int64_t)first_wire + t;
+
+  float I0[10], V0[9], ni[10], nv[11];
+#pragma unroll
+  for (int k = 0; k < 10; k++) I0[k] = cur[k * S + w];
+#pragma unroll
+  for (int k = 0; k < 9; k++) V0[k] = vol[k * S + w];
+  const uint32_t a = in_ptr[w], b = out_ptr[w];
+  const float v_out = pick_instance(out_loc[w], v_pvt, v_shr, v_ghost)[b];
+#pragma unroll
+  for (int k = 0; k < 10; k++) ni[k] = I0[k];
+  if (INIT == CKT_INIT_KERNEL) {
+    nv[0] = pick_instance(in_loc[w], v_pvt, v_shr, v_ghost)[a];
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k + 1] = V0[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k] = V0[k];
+    nv[9] = 0.0f;
+  }
+  nv[10] = v_out;
+
+  const WireStep<MODE> ws(Lw[w], Rw[w], Cw[w], dt);
+  int j = 0;
+#pragma unroll 1
+  for (; j + 2 <= steps; j += 2) {
+    ws.step(ni, nv, I0, V0);
+    ws.step(ni, nv, I0, V0);
+  }
+  if (j < steps) ws.step(ni, nv, I0, V0);
+
+#pragma unroll
+  for (int k = 0; k < 10; k++) cur[k * S + w] = ni[k];
+#pragma unroll
+  for (int k = 0; k < 9; k++) vol[k * S + w] = nv[k + 1];
+}
+
+// ---------------------------------------------------------------------------
+// distribute_charge.  The reference adds -dt*I[0] to the in-node and
+// +dt*I[9] to the out-node of every wire with atomicAdd (unordered).  Here
+// each node GATHERS its contributions from a static CSR whose order is the
+// reference CPU runtime's: wire order within a piece, private nodes updated
+// in place, shared/ghost contributions folded per piece (identity 0) and the
+// folds applied in ascending piece order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float contribution(uint32_t wire, uint32_t end,
+                                              const float *__restrict__ I0,
+                                              const float *__restrict__ I9, float dt) {
+  // -dt * current[0] (in end) and dt * current[9] (out end),
+  // apps/circuit/circuit.cc:430-431.
+  return end ? __fmul_rn(dt, I9[wire]) : __fmul_rn(-dt, I0[wire]);
+}
+
+// Whole circuit: one thread per node, canonical order.
+__global__ void __launch_bounds__(256)
+    dc_all_kernel(uint32_t N, const uint32_t *__restrict__ off, const uint32_t *__restrict__ ent,
+                  const float *__restrict__ I0, const float *__restrict__ I9,
+                  float *__restrict__ charge, float dt) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const uint32_t o0 = off[x], o1 = off[x + 1];
+  const uint32_t b = o0 & 0x7fffffffu, e = o1 & 0x7fffffffu;
+  float acc = charge[x];
+  if (o0 & 0x80000000u) {
+    for (uint32_t i = b; i < e; i++) {
+      const uint32_t u = ent[i];
+      acc = __fadd_rn(acc, contribution(u >> 2, (u >> 1) & 1u, I0, I9, dt));
+    }
+  } else {
+    float fold = 0.0f;
+    for (uint32_t i = b; i < e; i++) {
+      const uint32_t u = ent[i];
+      if ((u & 1u) && i != b) {
+        acc = __fadd_rn(acc, fold);
+        fold = 0.0f;
+      }
+      fold = __fadd_rn(fold, contribution(u >> 2, (u >> 1) & 1u, I0, I9, dt));
+    }
+    if (e > b) acc = __fadd_rn(acc, fold);
+  }
+  charge[x] = acc;
+}
+
+// One piece: one thread per node the piece touches; private nodes are
+// updated in place, shared/ghost nodes fold into the given instances.
+__global__ void __launch_bounds__(256)
+    dc_piece_kernel(uint32_t t0, uint32_t nt, const uint32_t *__restrict__ touch_node,
+                    const uint8_t *__restrict__ touch_loc, const uint32_t *__restrict__ touch_off,
+                    const uint32_t *__restrict__ pent, const float *__restrict__ I0,
+                    const float *__restrict__ I9, float *charge, float *shr_fold,
+                    float *ghost_fold, float dt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const uint32_t t = t0 + i;
+  const uint32_t x = touch_node[t];
+  const uint8_t loc = touch_loc[t];
+  float *tgt = loc == CKT_PRIVATE_PTR ? charge : (loc == CKT_SHARED_PTR ? shr_fold : ghost_fold);
+  float acc = tgt[x];
+  for (uint32_t e = touch_off[t]; e < touch_off[t + 1]; e++) {
+    const uint32_t u = pent[e];
+    acc = __fadd_rn(acc, contribution(u >> 1, u & 1u, I0, I9, dt));
+  }
+  tgt[x] = acc;
+}
+
+// Application of one piece's reduction instances.
+__global__ void __launch_bounds__(256)
+    apply_fold_kernel(uint32_t t0, uint32_t nt, const uint32_t *__restrict__ touch_node,
+                      const uint8_t *__restrict__ touch_loc, float *shr_fold, float *ghost_fold,
+                      float *charge) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const uint32_t t = t0 + i;
+  const uint8_t loc = touch_loc[t];
+  if (loc == CKT_PRIVATE_PTR) return;
+  const uint32_t x = touch_node[t];
+  float *fold = loc == CKT_SHARED_PTR ? shr_fold : ghost_fold;
+  charge[x] = __fadd_rn(charge[x], fold[x]);
+  fold[x] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// update_voltages: v += q/C; v *= (1 - leak); q = 0
+// (apps/circuit/circuit_gpu.cu:330-335, circuit.cc:1300-1302).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float uv_one(float v, float q, float c, float l) {
+  return __fmul_rn(__fadd_rn(v, __fdiv_rn(q, c)), __fsub_rn(1.0f, l));
+}
+
+// Whole node range, four nodes per thread with 16-byte loads and stores.
+__global__ void __launch_bounds__(256)
+    uv_all_vec4_kernel(uint32_t n4, float4 *__restrict__ q, float4 *__restrict__ v,
+                       const float4 *__restrict__ c, const float4 *__restrict__ l) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n4) return;
+  const float4 qq = q[i], vv = v[i], cc = c[i], ll = l[i];
+  float4 r;
+  r.x = uv_one(vv.x, qq.x, cc.x, ll.x);
+  r.y = uv_one(vv.y, qq.y, cc.y, ll.y);
+  r.z = uv_one(vv.z, qq.z, cc.z, ll.z);
+  r.w = uv_one(vv.w, qq.w, cc.w, ll.w);
+  v[i] = r;
+  q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(256)
+    uv_all_scalar_kernel(uint32_t first, uint32_t n, float *__restrict__ q, float *__restrict__ v,
+                         const float *__restrict__ c, const float *__restrict__ l) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t x = first + i;
+  v[x] = uv_one(v[x], q[x], c[x], l[x]);
+  q[x] = 0.0f;
+}
+
+// One piece, instance chosen by the locator (circuit_gpu.cu:321-346).
+__global__ void __launch_bounds__(256)
+    uv_piece_kernel(uint32_t first, uint32_t n, const int32_t *__restrict__ locator,
+                    ckt_nodes pvt, ckt_nodes shr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t x = first + i;
+  const ckt_nodes &s = locator[x] ? pvt : shr;
+  s.voltage[x] = uv_one(s.voltage[x], s.charge[x], s.capacitance[x], s.leakage[x]);
+  s.charge[x] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Wire validation (sanity_check_positions, circuit_gpu.cu:151-184, with an
+// error word instead of assert).  Records the smallest failing wire index.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    sanity_kernel(ckt_piece piece, const uint32_t *__restrict__ in_ptr,
+                  const uint32_t *__restrict__ out_ptr, const uint8_t *__restrict__ in_loc,
+                  const uint8_t *__restrict__ out_loc, uint32_t num_nodes_total,
+                  unsigned long long *first_bad) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= piece.num_wires) return;
+  const uint32_t w = piece.first_wire + t;
+  const uint32_t a = in_ptr[w], b = out_ptr[w];
+  const uint8_t la = in_loc[w], lb = out_loc[w];
+  const uint32_t lo = piece.first_node, hi = piece.first_node + piece.num_nodes;
+  bool ok = la <= CKT_SHARED_PTR && lb <= CKT_GHOST_PTR;  // in-node is never a ghost
+  ok = ok && a >= lo && a < hi;
+  ok = ok && b < num_nodes_total;
+  if (ok) {
+    const bool b_inside = b >= lo && b < hi;
+    ok = (lb == CKT_GHOST_PTR) ? !b_inside : b_inside;
+  }
+  if (!ok) atomicMin(first_bad, (unsigned long long)w);
+}
+
+}  // namespace ckt

@@ -1,0 +1,35 @@
+// ckt_probe.cu -- FP32-pipe peak probe used as the roofline denominator of
+// calc_new_currents (the measured-peak file holds HBM and tensor peaks only).
+// Eight independent FMA chains per thread keep all four SM sub-partitions'
+// FP32 pipes issuing every cycle.
+#include "ckt_internal.h"
+
+namespace ckt {
+
+__global__ void __launch_bounds__(256) fma_probe_kernel(int32_t iters, float *sink) {
+  float a[8];
+  const float m = 1.0f + 1e-7f * (threadIdx.x & 7), c = 1e-7f;
+#pragma unroll
+  for (int i = 0; i < 8; i++) a[i] = (float)(threadIdx.x + i);
+#pragma unroll 1
+  for (int32_t j = 0; j < iters; j++) {
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) a[i] = __fmaf_rn(a[i], m, c);
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; i++) s += a[i];
+  if (s == 12345.678f) sink[0] = s;  // keeps the chains live
+}
+
+}  // namespace ckt
+
+extern "C" int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, float *sink, void *stream) {
+  CKT_REQUIRE(blocks > 0 && iters > 0 && sink != nullptr, "bad probe arguments");
+  ckt::fma_probe_kernel<<<blocks, 256, 0, ckt::as_stream(stream)>>>(iters, sink);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}

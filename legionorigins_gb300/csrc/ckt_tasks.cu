@@ -1,0 +1,262 @@
+// ckt_tasks.cu -- C-ABI entry points of the three leaf tasks (per piece and
+// index-space), fold application and wire validation.
+#include <climits>
+#include <cstring>
+
+#include "ckt_internal.h"
+#include "ckt_kernels.cuh"
+
+namespace ckt {
+
+static thread_local std::string g_last_error;
+
+int set_error(int status, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+int validate_wires(const ckt_wires &w) {
+  CKT_REQUIRE(w.in_ptr && w.out_ptr && w.in_loc && w.out_loc, "wire pointer/location arrays are NULL");
+  CKT_REQUIRE(w.inductance && w.resistance && w.capacitance, "wire L/R/C arrays are NULL");
+  CKT_REQUIRE(w.current && w.voltage, "wire current/voltage arrays are NULL");
+  CKT_REQUIRE(w.seg_stride > 0, "wire seg_stride must be positive (got %lld)", (long long)w.seg_stride);
+  return CKT_OK;
+}
+
+int validate_nodes(const ckt_nodes &n, const char *what) {
+  CKT_REQUIRE(n.charge && n.voltage && n.capacitance && n.leakage, "%s node instance has NULL arrays",
+              what);
+  return CKT_OK;
+}
+
+int validate_params(const ckt_params *p) {
+  CKT_REQUIRE(p != nullptr, "params is NULL");
+  CKT_REQUIRE(p->steps >= 0, "steps must be >= 0 (got %d)", p->steps);
+  CKT_REQUIRE(p->mode == CKT_MODE_EXACT || p->mode == CKT_MODE_FAST, "unknown mode %d", p->mode);
+  CKT_REQUIRE(p->init == CKT_INIT_KERNEL || p->init == CKT_INIT_CPU_TASK, "unknown init %d", p->init);
+  return CKT_OK;
+}
+
+static inline unsigned grid_for(uint64_t n, unsigned block = 256) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+template <int M, int I>
+static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
+                         const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
+  cnc_kernel<M, I><<<grid_for(n), 256, 0, s>>>(first, n, w.in_ptr, w.out_ptr, w.in_loc, w.out_loc,
+                                               w.inductance, w.resistance, w.capacitance,
+                                               w.current, w.voltage, w.seg_stride, vp, vs, vg,
+                                               p->steps, p->dt);
+}
+
+static int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
+                      const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
+  if (n == 0) return CKT_OK;
+  CKT_REQUIRE((int64_t)first + n <= w.seg_stride,
+              "wire range [%u, %llu) exceeds seg_stride %lld", first,
+              (unsigned long long)first + n, (long long)w.seg_stride);
+  if (p->mode == CKT_MODE_EXACT) {
+    if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_EXACT, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
+    else launch_cnc_t<CKT_MODE_EXACT, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
+  } else {
+    if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_FAST, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
+    else launch_cnc_t<CKT_MODE_FAST, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
+  }
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+static int check_graph_wires(const ckt_graph *g, const ckt_wires &w) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  CKT_REQUIRE(w.seg_stride >= g->W, "wires.seg_stride %lld is smaller than the graph's %lld wires",
+              (long long)w.seg_stride, (long long)g->W);
+  return CKT_OK;
+}
+
+}  // namespace ckt
+
+using namespace ckt;
+
+extern "C" {
+
+int ckt_abi_version(void) { return CKT_ABI_VERSION; }
+
+const char *ckt_last_error(void) { return g_last_error.c_str(); }
+
+const char *ckt_status_string(int status) {
+  switch (status) {
+    case CKT_OK: return "ok";
+    case CKT_EINVAL: return "invalid argument";
+    case CKT_ECUDA: return "CUDA error";
+    case CKT_EBOUNDS: return "pointer or location out of bounds";
+    case CKT_ETIMEOUT: return "bounded device wait timed out";
+    case CKT_ENOMEM: return "out of memory or over budget";
+    case CKT_EBUSY: return "busy";
+    case CKT_ECANCELLED: return "cancelled";
+    default: return "unknown status";
+  }
+}
+
+void ckt_default_params(ckt_params *out) {
+  if (!out) return;
+  out->steps = 10000;
+  out->dt = (float)1e-6;
+  out->mode = CKT_MODE_EXACT;
+  out->init = CKT_INIT_KERNEL;
+}
+
+int ckt_calc_new_currents(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt, ckt_nodes shr,
+                          ckt_nodes ghost, const ckt_params *prm, void *stream) {
+  CKT_REQUIRE(piece != nullptr, "piece is NULL");
+  int rc;
+  if ((rc = validate_wires(wires)) || (rc = validate_params(prm))) return rc;
+  CKT_REQUIRE(pvt.voltage && shr.voltage && ghost.voltage, "node voltage arrays are NULL");
+  return launch_cnc(piece->first_wire, piece->num_wires, wires, pvt.voltage, shr.voltage,
+                    ghost.voltage, prm, as_stream(stream));
+}
+
+int ckt_calc_new_currents_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream) {
+  int rc;
+  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
+      (rc = check_graph_wires(graph, wires)))
+    return rc;
+  CKT_REQUIRE(nodes.voltage != nullptr, "node voltage array is NULL");
+  return launch_cnc(0, (uint32_t)graph->W, wires, nodes.voltage, nodes.voltage, nodes.voltage, prm,
+                    as_stream(stream));
+}
+
+int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires wires,
+                          ckt_nodes pvt, float *shr_fold, float *ghost_fold,
+                          const ckt_params *prm, void *stream) {
+  int rc;
+  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
+      (rc = check_graph_wires(graph, wires)))
+    return rc;
+  CKT_REQUIRE(piece_index >= 0 && piece_index < graph->P, "piece_index %d out of range [0, %d)",
+              piece_index, graph->P);
+  CKT_REQUIRE(pvt.charge != nullptr, "pvt.charge is NULL");
+  const int64_t t0 = graph->touch_first[piece_index], t1 = graph->touch_first[piece_index + 1];
+  if (t1 == t0) return CKT_OK;
+  CKT_REQUIRE(shr_fold != nullptr && ghost_fold != nullptr, "fold instances are NULL");
+  const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
+  dc_piece_kernel<<<grid_for(t1 - t0), 256, 0, as_stream(stream)>>>(
+      (uint32_t)t0, (uint32_t)(t1 - t0), graph->touch_node, graph->touch_loc, graph->touch_off,
+      graph->piece_ent, I0, I9, pvt.charge, shr_fold, ghost_fold, prm->dt);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+int ckt_apply_fold(const ckt_graph *graph, int32_t piece_index, float *shr_fold, float *ghost_fold,
+                   float *charge, void *stream) {
+  CKT_REQUIRE(graph != nullptr, "graph is NULL");
+  CKT_REQUIRE(piece_index >= 0 && piece_index < graph->P, "piece_index %d out of range [0, %d)",
+              piece_index, graph->P);
+  CKT_REQUIRE(shr_fold && ghost_fold && charge, "NULL fold or charge array");
+  const int64_t t0 = graph->touch_first[piece_index], t1 = graph->touch_first[piece_index + 1];
+  if (t1 == t0) return CKT_OK;
+  apply_fold_kernel<<<grid_for(t1 - t0), 256, 0, as_stream(stream)>>>(
+      (uint32_t)t0, (uint32_t)(t1 - t0), graph->touch_node, graph->touch_loc, shr_fold, ghost_fold,
+      charge);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream) {
+  int rc;
+  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
+      (rc = check_graph_wires(graph, wires)))
+    return rc;
+  CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
+  if (graph->N == 0) return CKT_OK;
+  const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
+  dc_all_kernel<<<grid_for(graph->N), 256, 0, as_stream(stream)>>>(
+      (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, prm->dt);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+int ckt_update_voltages(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
+                        const int32_t *locator, void *stream) {
+  CKT_REQUIRE(piece != nullptr, "piece is NULL");
+  int rc;
+  if ((rc = validate_nodes(pvt, "pvt")) || (rc = validate_nodes(shr, "shr"))) return rc;
+  CKT_REQUIRE(locator != nullptr, "locator is NULL");
+  if (piece->num_nodes == 0) return CKT_OK;
+  uv_piece_kernel<<<grid_for(piece->num_nodes), 256, 0, as_stream(stream)>>>(
+      piece->first_node, piece->num_nodes, locator, pvt, shr);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *stream) {
+  CKT_REQUIRE(graph != nullptr, "graph is NULL");
+  int rc;
+  if ((rc = validate_nodes(nodes, "nodes"))) return rc;
+  const uint64_t N = (uint64_t)graph->N;
+  if (N == 0) return CKT_OK;
+  const cudaStream_t s = as_stream(stream);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(nodes.charge) |
+                         reinterpret_cast<uintptr_t>(nodes.voltage) |
+                         reinterpret_cast<uintptr_t>(nodes.capacitance) |
+                         reinterpret_cast<uintptr_t>(nodes.leakage)) &
+                        15u) == 0;
+  uint64_t done = 0;
+  if (aligned && N >= 4) {
+    const uint64_t n4 = N / 4;
+    uv_all_vec4_kernel<<<grid_for(n4), 256, 0, s>>>(
+        (uint32_t)n4, reinterpret_cast<float4 *>(nodes.charge),
+        reinterpret_cast<float4 *>(nodes.voltage),
+        reinterpret_cast<const float4 *>(nodes.capacitance),
+        reinterpret_cast<const float4 *>(nodes.leakage));
+    CKT_CHECK_LAUNCH();
+    done = n4 * 4;
+  }
+  if (done < N) {
+    uv_all_scalar_kernel<<<grid_for(N - done), 256, 0, s>>>(
+        (uint32_t)done, (uint32_t)(N - done), nodes.charge, nodes.voltage, nodes.capacitance,
+        nodes.leakage);
+    CKT_CHECK_LAUNCH();
+  }
+  return CKT_OK;
+}
+
+int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num_nodes_total,
+                           int64_t *first_bad, void *stream) {
+  CKT_REQUIRE(piece != nullptr, "piece is NULL");
+  CKT_REQUIRE(wires.in_ptr && wires.out_ptr && wires.in_loc && wires.out_loc,
+              "wire pointer/location arrays are NULL");
+  if (first_bad) *first_bad = -1;
+  if (piece->num_wires == 0) return CKT_OK;
+  const cudaStream_t s = as_stream(stream);
+  unsigned long long *d_bad = nullptr;
+  CKT_CUDA(cudaMallocAsync(&d_bad, sizeof(unsigned long long), s));
+  const unsigned long long none = ULLONG_MAX;
+  unsigned long long h_bad = none;
+  int rc = CKT_OK;
+  cudaError_t e = cudaMemcpyAsync(d_bad, &none, sizeof(none), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    sanity_kernel<<<grid_for(piece->num_wires), 256, 0, s>>>(*piece, wires.in_ptr, wires.out_ptr,
+                                                              wires.in_loc, wires.out_loc,
+                                                              num_nodes_total, d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFreeAsync(d_bad, s);
+  if (e != cudaSuccess) return set_error(CKT_ECUDA, "sanity check failed: %s", cudaGetErrorString(e));
+  if (h_bad != none) {
+    if (first_bad) *first_bad = (int64_t)h_bad;
+    rc = set_error(CKT_EBOUNDS, "wire %llu fails the pointer/location checks", h_bad);
+  }
+  return rc;
+}
+
+}  // extern "C"
