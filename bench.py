@@ -56,7 +56,10 @@ L_OFFSET, L_SCALE = 0.001, 0.01
 FLOPS_PER_WIRE_STEP = 96  # the reference's own count (apps/circuit/circuit.cc:324)
 
 
-def workload_config(mode: str) -> dict:
+def workload_config(mode: str, pieces: int = SHAPE["num_pieces"]) -> dict:
+    if pieces != SHAPE["num_pieces"]:
+        return {"workload": f"PROFILING CASE, not the configured workload: {pieces} pieces x "
+                            f"16384 nodes x 65536 wires/piece, S=1000 x 10 loops", "mode": mode}
     return {
         "workload": "plain circuit at scale: 64 pieces x 16384 nodes x 65536 wires/piece "
                     "(4,194,304 wires), 95% in-piece, 10 segments, S=1000 inner steps x "
@@ -225,6 +228,8 @@ def main() -> None:
     ap.add_argument("--cpu-sample-s", type=float, default=3.0,
                     help="target seconds of CPU work per sampled step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
+                    help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -265,7 +270,7 @@ def main() -> None:
                       f"restated in C (oracle/ckt_oracle.c), {threads} threads",
         }
 
-    shape = C.Shape(**SHAPE)
+    shape = C.Shape(args.pieces, SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"])
     host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
                       SEED + 0, L_OFFSET, L_SCALE)
     dc = C.DeviceCircuit(host, shape, device=f"cuda:{local}")
@@ -404,7 +409,7 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (reference generator distributions, seed 12345)",
-            "config": workload_config(args.mode), "roofline": roofline,
+            "config": workload_config(args.mode, shape.num_pieces), "roofline": roofline,
             "cpu_baseline": cpu_baseline, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "kernels": kernels,
             "replicas": "one independent circuit per GPU" if ws > 1 else None,

@@ -143,7 +143,11 @@ int ckt_calc_new_currents(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt
  * `graph`: private nodes' charge is updated in place in wire order
  * (apply<true>); shared and ghost nodes fold into `shr_fold` / `ghost_fold`
  * (float per absolute node index, the reduction instances of
- * runtime/lowlevel.h:835-881) in wire order.  Deterministic: no atomics. */
+ * runtime/lowlevel.h:835-881) in wire order.  Deterministic: no atomics.
+ * Like the reference's per-task reduction instances, the folds must hold
+ * the identity (0) for every node this piece touches: give each piece its
+ * own fold buffers, or apply this piece's folds with ckt_apply_fold (which
+ * resets them) before the next piece deposits into the same buffers. */
 int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires wires,
                           ckt_nodes pvt, float *shr_fold, float *ghost_fold,
                           const ckt_params *prm, void *stream);
@@ -226,6 +230,75 @@ typedef struct {
 } ckt_host_circuit;
 
 int ckt_generate(const ckt_gen_params *p, ckt_host_circuit *out);
+
+/* ------------------------------------------------------------------------
+ * Batched form: many independent circuits of uneven sizes.  One call of
+ * ckt_batch_run advances EVERY circuit by one outer loop (calc_new_currents
+ * with the circuit's own inner-step count, then distribute_charge, then
+ * update_voltages) in ONE persistent kernel launch, replayed from a CUDA
+ * graph.  Circuits are independent, so each one's results are bit-identical
+ * to running it alone with the index-space calls.  No counterpart in the
+ * reference, which runs one circuit per process.
+ * ---------------------------------------------------------------------- */
+typedef struct ckt_batch ckt_batch;
+
+/* Launch shape of the persistent kernel; chosen by ckt_batch_autotune. */
+typedef struct {
+  int32_t block;            /* threads per block: 128 or 256 */
+  int32_t wires_per_thread; /* calc_new_currents wires per thread per tile: 1 or 2 */
+  int32_t dc_schedule;      /* distribute_charge: 0 staged block gather, 1 thread per node */
+  int32_t blocks_per_sm;    /* output: resident blocks per SM of the persistent grid */
+} ckt_batch_config;
+
+/* From host circuits (each sized by its shape; node pointers local to the
+ * circuit).  steps[i] is circuit i's inner-step count. */
+int ckt_batch_create(int32_t num_circuits, const ckt_gen_params *shapes,
+                     const ckt_host_circuit *circuits, const int32_t *steps, ckt_batch **out);
+/* Same, generating every circuit with the reference generator (in parallel
+ * on `host_threads` threads). */
+int ckt_batch_generate(int32_t num_circuits, const ckt_gen_params *shapes, const int32_t *steps,
+                       int32_t host_threads, ckt_batch **out);
+int ckt_batch_destroy(ckt_batch *batch);
+/* Union sizes, wire-segment updates per run (sum of W x 10 x steps) and
+ * device bytes held. */
+int ckt_batch_info(const ckt_batch *batch, int64_t *num_wires, int64_t *num_nodes,
+                   double *segment_updates_per_run, int64_t *device_bytes);
+int ckt_batch_circuit_offsets(const ckt_batch *batch, int32_t circuit, int64_t *first_wire,
+                              int64_t *first_node);
+int ckt_batch_set_config(ckt_batch *batch, const ckt_batch_config *config);
+int ckt_batch_get_config(const ckt_batch *batch, ckt_batch_config *config);
+/* Times every launch shape on this batch (running it; the state is reset
+ * afterwards), keeps the fastest and caches it per shape bucket. */
+int ckt_batch_autotune(ckt_batch *batch, int32_t mode, void *stream, ckt_batch_config *chosen);
+/* One outer loop of every circuit: one persistent launch through a CUDA
+ * graph (captured on first use per mode). */
+int ckt_batch_run(ckt_batch *batch, int32_t mode, void *stream);
+/* Same launch without the graph. */
+int ckt_batch_run_direct(ckt_batch *batch, int32_t mode, void *stream);
+/* The plain path on the same batch: circuit after circuit, three launches
+ * each (the comparison point of the batched form). */
+int ckt_batch_run_sequential(ckt_batch *batch, int32_t mode, void *stream);
+/* Synchronises `stream` and reads the persistent kernel's error word:
+ * CKT_ETIMEOUT if a bounded wait ran out. */
+int ckt_batch_check(ckt_batch *batch, void *stream);
+/* Bound of every device-side wait (default 2 s). */
+int ckt_batch_set_timeout(ckt_batch *batch, uint64_t timeout_ns);
+/* Restores the state the batch was created with. */
+int ckt_batch_reset_state(ckt_batch *batch, void *stream);
+/* Circuit `circuit`'s state to host arrays ([10][W_i], [9][W_i], [N_i],
+ * [N_i]); NULL skips a field.  Synchronous. */
+int ckt_batch_read_state(ckt_batch *batch, int32_t circuit, float *current, float *voltage,
+                         float *charge, float *node_voltage, void *stream);
+/* Whole-union state from / to host memory (sizes from ckt_batch_info;
+ * asynchronous on `stream`; pinned host memory gives full copy speed). */
+int ckt_batch_upload_state(ckt_batch *batch, const float *current, const float *voltage,
+                           const float *charge, const float *node_voltage, void *stream);
+int ckt_batch_download_state(ckt_batch *batch, float *current, float *voltage, float *charge,
+                             float *node_voltage, void *stream);
+/* Fault injection for tests: makes circuit `circuit`'s distribute_charge
+ * tiles wait for a calc_new_currents tile that does not exist, so the wait
+ * runs out (enable = 0 restores the table). */
+int ckt_batch_inject_stall(ckt_batch *batch, int32_t circuit, int32_t enable);
 
 /* ------------------------------------------------------------------------
  * Measurement helper (no counterpart in the reference): FP32 FMA throughput

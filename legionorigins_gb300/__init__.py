@@ -66,6 +66,11 @@ class HostCircuit(ctypes.Structure):
         "locator")]
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("wires_per_thread", ctypes.c_int32),
+                ("dc_schedule", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32)]
+
+
 # (name, restype, argtypes) of every exported symbol declared in include/ckt.h
 _P = ctypes.c_void_p
 _I32, _I64, _U32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32
@@ -92,6 +97,29 @@ SIGNATURES = {
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
     "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _P, _P]),
+    "ckt_batch_create": (ctypes.c_int, [_I32, ctypes.POINTER(GenParams),
+                                        ctypes.POINTER(HostCircuit), ctypes.POINTER(_I32),
+                                        ctypes.POINTER(_P)]),
+    "ckt_batch_generate": (ctypes.c_int, [_I32, ctypes.POINTER(GenParams), ctypes.POINTER(_I32),
+                                          _I32, ctypes.POINTER(_P)]),
+    "ckt_batch_destroy": (ctypes.c_int, [_P]),
+    "ckt_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)]),
+    "ckt_batch_circuit_offsets": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_I64),
+                                                 ctypes.POINTER(_I64)]),
+    "ckt_batch_set_config": (ctypes.c_int, [_P, ctypes.POINTER(BatchConfig)]),
+    "ckt_batch_get_config": (ctypes.c_int, [_P, ctypes.POINTER(BatchConfig)]),
+    "ckt_batch_autotune": (ctypes.c_int, [_P, _I32, _P, ctypes.POINTER(BatchConfig)]),
+    "ckt_batch_run": (ctypes.c_int, [_P, _I32, _P]),
+    "ckt_batch_run_direct": (ctypes.c_int, [_P, _I32, _P]),
+    "ckt_batch_run_sequential": (ctypes.c_int, [_P, _I32, _P]),
+    "ckt_batch_check": (ctypes.c_int, [_P, _P]),
+    "ckt_batch_set_timeout": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "ckt_batch_reset_state": (ctypes.c_int, [_P, _P]),
+    "ckt_batch_read_state": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P]),
+    "ckt_batch_upload_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "ckt_batch_download_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "ckt_batch_inject_stall": (ctypes.c_int, [_P, _I32, _I32]),
 }
 
 _lib = None

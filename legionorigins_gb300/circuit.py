@@ -152,8 +152,11 @@ class DeviceCircuit:
 
     def loop_per_piece(self, prm: Params, stream: int = 0) -> None:
         """One outer loop as the reference's per-piece task calls: CNC for
-        every piece, DC for every piece (then the runtime's fold application,
-        pieces ascending), UV for every piece."""
+        every piece; DC for every piece, each followed by the application of
+        that piece's reduction instances (the runtime applies a point's
+        instances once the point finishes, points in ascending order; the
+        two fold buffers are reused, and ckt_apply_fold returns them to the
+        identity); UV for every piece."""
         L, g, w, n = lib(), self.graph.handle, self.wires(), self.nodes()
         locator = self.t["locator"].data_ptr()
         for k in range(len(self.pieces)):
@@ -162,7 +165,6 @@ class DeviceCircuit:
         sf, gf = self.shr_fold.data_ptr(), self.ghost_fold.data_ptr()
         for k in range(len(self.pieces)):
             check(L.ckt_distribute_charge(g, k, w, n, sf, gf, ctypes.byref(prm), stream))
-        for k in range(len(self.pieces)):
             check(L.ckt_apply_fold(g, k, sf, gf, n.charge, stream))
         for k in range(len(self.pieces)):
             check(L.ckt_update_voltages(ctypes.byref(self.pieces[k]), n, n, locator, stream))

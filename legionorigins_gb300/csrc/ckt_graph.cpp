@@ -45,13 +45,12 @@ static void free_graph(ckt_graph *g) {
 
 using namespace ckt;
 
-extern "C" {
+namespace ckt {
 
-int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
-                     const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
-                     const uint8_t *out_loc, ckt_graph **out) {
-  CKT_REQUIRE(out != nullptr, "out is NULL");
-  *out = nullptr;
+int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
+                   const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
+                   const uint8_t *out_loc, std::vector<uint32_t> &off, std::vector<uint32_t> &ent,
+                   int64_t *num_wires) {
   CKT_REQUIRE(num_pieces >= 1 && pieces != nullptr, "need at least one piece");
   // Pieces tile [0, W) in order; node ranges lie inside [0, N) and are disjoint.
   int64_t W = 0;
@@ -104,15 +103,10 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
     }
   }
 
-  ckt_graph *g = new ckt_graph();
-  g->W = W;
-  g->N = N;
-  g->P = num_pieces;
-  g->pieces.assign(pieces, pieces + num_pieces);
-
   // Whole-circuit CSR: counting sort of the 2W endpoints by node; filling in
   // wire order keeps (wire, end) order inside each node.
-  std::vector<uint32_t> off(N + 1, 0), ent(2 * W);
+  off.assign(N + 1, 0);
+  ent.assign(2 * W, 0);
   for (int64_t w = 0; w < W; w++) {
     off[in_ptr[w] + 1]++;
     off[out_ptr[w] + 1]++;
@@ -136,6 +130,30 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
   }
   for (int64_t x = 0; x < N; x++)
     if (kind[x] != 2) off[x] |= kPrivateBit;
+  if (num_wires) *num_wires = W;
+  return CKT_OK;
+}
+
+}  // namespace ckt
+
+extern "C" {
+
+int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
+                     const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
+                     const uint8_t *out_loc, ckt_graph **out) {
+  CKT_REQUIRE(out != nullptr, "out is NULL");
+  *out = nullptr;
+  std::vector<uint32_t> off, ent;
+  int64_t W = 0;
+  int rc = build_node_csr(pieces, num_pieces, num_nodes, in_ptr, out_ptr, in_loc, out_loc, off,
+                          ent, &W);
+  if (rc) return rc;
+
+  ckt_graph *g = new ckt_graph();
+  g->W = W;
+  g->N = num_nodes;
+  g->P = num_pieces;
+  g->pieces.assign(pieces, pieces + num_pieces);
 
   // Per-piece CSR over touched nodes, nodes ascending, wire order inside.
   std::vector<uint32_t> touch_node, touch_off, pent;
@@ -168,7 +186,6 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
   g->touch_first[num_pieces] = (int64_t)touch_node.size();
   touch_off.push_back((uint32_t)pent.size());
 
-  int rc = CKT_OK;
   if ((rc = upload(&g->node_off, off, &g->device_bytes)) ||
       (rc = upload(&g->node_ent, ent, &g->device_bytes)) ||
       (rc = upload(&g->touch_node, touch_node, &g->device_bytes)) ||

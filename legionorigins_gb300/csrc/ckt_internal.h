@@ -47,6 +47,21 @@ constexpr uint32_t kPrivateBit = 0x80000000u;
 constexpr uint32_t kOffsetMask = 0x7fffffffu;
 constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 31 bits
 
+inline unsigned grid_for(uint64_t n, unsigned block = 256) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+// Validates the wires against the pieces and builds the whole-circuit CSR
+// (node offsets with the private bit, entries in reduction order).
+int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
+                   const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
+                   const uint8_t *out_loc, std::vector<uint32_t> &off, std::vector<uint32_t> &ent,
+                   int64_t *num_wires);
+
+// calc_new_currents over wires [first, first + n) (any mode/initialisation).
+int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp, const float *vs,
+               const float *vg, const ckt_params *p, cudaStream_t s);
+
 int validate_wires(const ckt_wires &w);
 int validate_nodes(const ckt_nodes &n, const char *what);
 int validate_params(const ckt_params *p);

@@ -77,30 +77,34 @@ __device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *
   return loc == CKT_PRIVATE_PTR ? pvt : (loc == CKT_SHARED_PTR ? shr : ghost);
 }
 
-template <int MODE, int INIT>
-__global__ void __launch_bounds__(256)
-    cnc_kernel(uint32_t first_wire, uint32_t num_wires, const uint32_t *__restrict__ in_ptr,
-               const uint32_t *__restrict__ out_ptr, const uint8_t *__restrict__ in_loc,
-               const uint8_t *__restrict__ out_loc, const float *__restrict__ Lw,
-               const float *__restrict__ Rw, const float *__restrict__ Cw,
-               float *__restrict__ cur, float *__restrict__ vol, int64_t S,
-               const float *__restrict__ v_pvt, const float *__restrict__ v_shr,
-               const float *__restrict__ v_ghost, int steps, float dt) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= num_wires) return;
-  const int64_t w = (int64_t)first_wire + t;
+// Device views of the wire region and of the node voltages CNC reads.
+struct WireArrays {
+  const uint32_t *in_ptr, *out_ptr;
+  const uint8_t *in_loc, *out_loc;
+  const float *L, *R, *C;
+  float *cur, *vol;
+  int64_t S;  // segment stride
+};
+struct NodeVolts {
+  const float *pvt, *shr, *ghost;
+};
 
+// One wire's whole inner loop: load, S steps in registers, store.
+template <int MODE, int INIT>
+__device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const NodeVolts &nv_in,
+                                         int steps, float dt) {
+  const int64_t S = a.S;
   float I0[10], V0[9], ni[10], nv[11];
 #pragma unroll
-  for (int k = 0; k < 10; k++) I0[k] = cur[k * S + w];
+  for (int k = 0; k < 10; k++) I0[k] = a.cur[k * S + w];
 #pragma unroll
-  for (int k = 0; k < 9; k++) V0[k] = vol[k * S + w];
-  const uint32_t a = in_ptr[w], b = out_ptr[w];
-  const float v_out = pick_instance(out_loc[w], v_pvt, v_shr, v_ghost)[b];
+  for (int k = 0; k < 9; k++) V0[k] = a.vol[k * S + w];
+  const uint32_t in = a.in_ptr[w], out = a.out_ptr[w];
+  const float v_out = pick_instance(a.out_loc[w], nv_in.pvt, nv_in.shr, nv_in.ghost)[out];
 #pragma unroll
   for (int k = 0; k < 10; k++) ni[k] = I0[k];
   if (INIT == CKT_INIT_KERNEL) {
-    nv[0] = pick_instance(in_loc[w], v_pvt, v_shr, v_ghost)[a];
+    nv[0] = pick_instance(a.in_loc[w], nv_in.pvt, nv_in.shr, nv_in.ghost)[in];
 #pragma unroll
     for (int k = 0; k < 9; k++) nv[k + 1] = V0[k];
   } else {
@@ -110,7 +114,7 @@ __global__ void __launch_bounds__(256)
   }
   nv[10] = v_out;
 
-  const WireStep<MODE> ws(Lw[w], Rw[w], Cw[w], dt);
+  const WireStep<MODE> ws(a.L[w], a.R[w], a.C[w], dt);
   int j = 0;
 #pragma unroll 1
   for (; j + 2 <= steps; j += 2) {
@@ -120,9 +124,18 @@ __global__ void __launch_bounds__(256)
   if (j < steps) ws.step(ni, nv, I0, V0);
 
 #pragma unroll
-  for (int k = 0; k < 10; k++) cur[k * S + w] = ni[k];
+  for (int k = 0; k < 10; k++) a.cur[k * S + w] = ni[k];
 #pragma unroll
-  for (int k = 0; k < 9; k++) vol[k * S + w] = nv[k + 1];
+  for (int k = 0; k < 9; k++) a.vol[k * S + w] = nv[k + 1];
+}
+
+template <int MODE, int INIT>
+__global__ void __launch_bounds__(256)
+    cnc_kernel(uint32_t first_wire, uint32_t num_wires, WireArrays a, NodeVolts v, int steps,
+               float dt) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= num_wires) return;
+  cnc_wire<MODE, INIT>((int64_t)first_wire + t, a, v, steps, dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -141,39 +154,120 @@ __device__ __forceinline__ float contribution(uint32_t wire, uint32_t end,
   return end ? __fmul_rn(dt, I9[wire]) : __fmul_rn(-dt, I0[wire]);
 }
 
-// Whole circuit: one thread per node, canonical order.
-__global__ void __launch_bounds__(256)
-    dc_all_kernel(uint32_t N, const uint32_t *__restrict__ off, const uint32_t *__restrict__ ent,
-                  const float *__restrict__ I0, const float *__restrict__ I9,
-                  float *__restrict__ charge, float dt) {
-  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= N) return;
+// Whole circuit, canonical order.  A block owns BLOCK consecutive nodes,
+// whose contributions are one contiguous span of the CSR.  The block first
+// stages the span in shared memory -- coalesced entry loads and independent
+// current gathers, so every thread has many loads in flight -- then each
+// thread sums its own node's run sequentially, in the reference order.
+// COHERENT loads bypass L1: used when the currents were written by other
+// blocks of the same (persistent) launch.
+constexpr uint32_t kDcChunk = 4096;
+
+template <bool COHERENT>
+__device__ __forceinline__ float ld_f32(const float *p) {
+  return COHERENT ? __ldcg(p) : *p;
+}
+
+template <uint32_t BLOCK, bool COHERENT>
+__device__ __forceinline__ void dc_block(uint32_t x0, uint32_t xe,
+                                         const uint32_t *__restrict__ off,
+                                         const uint32_t *__restrict__ ent,
+                                         const float *__restrict__ I0,
+                                         const float *__restrict__ I9,
+                                         float *__restrict__ charge, float dt, float *sval,
+                                         uint8_t *sflag) {
+  const uint32_t x = x0 + threadIdx.x;
+  const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
+  uint32_t b = 0, e = 0;
+  bool priv = true;
+  float acc = 0.0f, fold = 0.0f;
+  if (x < xe) {
+    const uint32_t o0 = off[x], o1 = off[x + 1];
+    priv = (o0 & 0x80000000u) != 0;
+    b = o0 & 0x7fffffffu;
+    e = o1 & 0x7fffffffu;
+    acc = charge[x];
+  }
+  for (uint32_t c0 = lo; c0 < hi; c0 += kDcChunk) {
+    const uint32_t cn = min(kDcChunk, hi - c0);
+#pragma unroll 4
+    for (uint32_t j = threadIdx.x; j < cn; j += BLOCK) {
+      const uint32_t u = ent[c0 + j];
+      const uint32_t w = u >> 2;
+      sval[j] = (u & 2u) ? __fmul_rn(dt, ld_f32<COHERENT>(I9 + w))
+                         : __fmul_rn(-dt, ld_f32<COHERENT>(I0 + w));
+      sflag[j] = (uint8_t)(u & 1u);
+    }
+    __syncthreads();
+    const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
+    if (priv) {
+      for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sval[i - c0]);
+    } else {
+      for (uint32_t i = i0; i < i1; i++) {
+        if (sflag[i - c0] && i != b) {
+          acc = __fadd_rn(acc, fold);
+          fold = 0.0f;
+        }
+        fold = __fadd_rn(fold, sval[i - c0]);
+      }
+    }
+    __syncthreads();
+  }
+  if (x < xe) {
+    if (!priv && e > b) acc = __fadd_rn(acc, fold);
+    charge[x] = acc;
+  }
+}
+
+// The simple schedule: one thread per node walks its own run with dependent
+// loads (no staging).  Same order, same bits.
+template <bool COHERENT>
+__device__ __forceinline__ void dc_node(uint32_t x, const uint32_t *__restrict__ off,
+                                        const uint32_t *__restrict__ ent,
+                                        const float *__restrict__ I0,
+                                        const float *__restrict__ I9,
+                                        float *__restrict__ charge, float dt) {
   const uint32_t o0 = off[x], o1 = off[x + 1];
   const uint32_t b = o0 & 0x7fffffffu, e = o1 & 0x7fffffffu;
   float acc = charge[x];
   if (o0 & 0x80000000u) {
     for (uint32_t i = b; i < e; i++) {
-      const uint32_t u = ent[i];
-      acc = __fadd_rn(acc, contribution(u >> 2, (u >> 1) & 1u, I0, I9, dt));
+      const uint32_t u = ent[i], w = u >> 2;
+      acc = __fadd_rn(acc, (u & 2u) ? __fmul_rn(dt, ld_f32<COHERENT>(I9 + w))
+                                    : __fmul_rn(-dt, ld_f32<COHERENT>(I0 + w)));
     }
   } else {
     float fold = 0.0f;
     for (uint32_t i = b; i < e; i++) {
-      const uint32_t u = ent[i];
+      const uint32_t u = ent[i], w = u >> 2;
       if ((u & 1u) && i != b) {
         acc = __fadd_rn(acc, fold);
         fold = 0.0f;
       }
-      fold = __fadd_rn(fold, contribution(u >> 2, (u >> 1) & 1u, I0, I9, dt));
+      fold = __fadd_rn(fold, (u & 2u) ? __fmul_rn(dt, ld_f32<COHERENT>(I9 + w))
+                                      : __fmul_rn(-dt, ld_f32<COHERENT>(I0 + w)));
     }
     if (e > b) acc = __fadd_rn(acc, fold);
   }
   charge[x] = acc;
 }
 
+constexpr uint32_t kDcBlock = 256;
+
+static __global__ void __launch_bounds__(kDcBlock)
+    dc_all_kernel(uint32_t node_begin, uint32_t node_end, const uint32_t *__restrict__ off,
+                  const uint32_t *__restrict__ ent, const float *__restrict__ I0,
+                  const float *__restrict__ I9, float *__restrict__ charge, float dt) {
+  __shared__ float sval[kDcChunk];
+  __shared__ uint8_t sflag[kDcChunk];
+  const uint32_t x0 = node_begin + blockIdx.x * kDcBlock;
+  dc_block<kDcBlock, false>(x0, min(node_end, x0 + kDcBlock), off, ent, I0, I9, charge, dt, sval,
+                            sflag);
+}
+
 // One piece: one thread per node the piece touches; private nodes are
 // updated in place, shared/ghost nodes fold into the given instances.
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     dc_piece_kernel(uint32_t t0, uint32_t nt, const uint32_t *__restrict__ touch_node,
                     const uint8_t *__restrict__ touch_loc, const uint32_t *__restrict__ touch_off,
                     const uint32_t *__restrict__ pent, const float *__restrict__ I0,
@@ -194,7 +288,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // Application of one piece's reduction instances.
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     apply_fold_kernel(uint32_t t0, uint32_t nt, const uint32_t *__restrict__ touch_node,
                       const uint8_t *__restrict__ touch_loc, float *shr_fold, float *ghost_fold,
                       float *charge) {
@@ -218,7 +312,7 @@ __device__ __forceinline__ float uv_one(float v, float q, float c, float l) {
 }
 
 // Whole node range, four nodes per thread with 16-byte loads and stores.
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     uv_all_vec4_kernel(uint32_t n4, float4 *__restrict__ q, float4 *__restrict__ v,
                        const float4 *__restrict__ c, const float4 *__restrict__ l) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,7 +327,7 @@ __global__ void __launch_bounds__(256)
   q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     uv_all_scalar_kernel(uint32_t first, uint32_t n, float *__restrict__ q, float *__restrict__ v,
                          const float *__restrict__ c, const float *__restrict__ l) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -244,7 +338,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // One piece, instance chosen by the locator (circuit_gpu.cu:321-346).
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     uv_piece_kernel(uint32_t first, uint32_t n, const int32_t *__restrict__ locator,
                     ckt_nodes pvt, ckt_nodes shr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -259,7 +353,7 @@ __global__ void __launch_bounds__(256)
 // Wire validation (sanity_check_positions, circuit_gpu.cu:151-184, with an
 // error word instead of assert).  Records the smallest failing wire index.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
     sanity_kernel(ckt_piece piece, const uint32_t *__restrict__ in_ptr,
                   const uint32_t *__restrict__ out_ptr, const uint8_t *__restrict__ in_loc,
                   const uint8_t *__restrict__ out_loc, uint32_t num_nodes_total,

@@ -42,20 +42,30 @@ int validate_params(const ckt_params *p) {
   return CKT_OK;
 }
 
-static inline unsigned grid_for(uint64_t n, unsigned block = 256) {
-  return (unsigned)((n + block - 1) / block);
+WireArrays wire_arrays(const ckt_wires &w) {
+  WireArrays a;
+  a.in_ptr = w.in_ptr;
+  a.out_ptr = w.out_ptr;
+  a.in_loc = w.in_loc;
+  a.out_loc = w.out_loc;
+  a.L = w.inductance;
+  a.R = w.resistance;
+  a.C = w.capacitance;
+  a.cur = w.current;
+  a.vol = w.voltage;
+  a.S = w.seg_stride;
+  return a;
 }
 
 template <int M, int I>
 static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
                          const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
-  cnc_kernel<M, I><<<grid_for(n), 256, 0, s>>>(first, n, w.in_ptr, w.out_ptr, w.in_loc, w.out_loc,
-                                               w.inductance, w.resistance, w.capacitance,
-                                               w.current, w.voltage, w.seg_stride, vp, vs, vg,
-                                               p->steps, p->dt);
+  const WireArrays a = wire_arrays(w);
+  const NodeVolts v = {vp, vs, vg};
+  cnc_kernel<M, I><<<grid_for(n), 256, 0, s>>>(first, n, a, v, p->steps, p->dt);
 }
 
-static int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
+int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
                       const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
   if (n == 0) return CKT_OK;
   CKT_REQUIRE((int64_t)first + n <= w.seg_stride,
@@ -115,7 +125,9 @@ int ckt_calc_new_currents(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt
                           ckt_nodes ghost, const ckt_params *prm, void *stream) {
   CKT_REQUIRE(piece != nullptr, "piece is NULL");
   int rc;
-  if ((rc = validate_wires(wires)) || (rc = validate_params(prm))) return rc;
+  if ((rc = validate_params(prm))) return rc;
+  if (piece->num_wires == 0) return CKT_OK;
+  if ((rc = validate_wires(wires))) return rc;
   CKT_REQUIRE(pvt.voltage && shr.voltage && ghost.voltage, "node voltage arrays are NULL");
   return launch_cnc(piece->first_wire, piece->num_wires, wires, pvt.voltage, shr.voltage,
                     ghost.voltage, prm, as_stream(stream));
@@ -124,9 +136,10 @@ int ckt_calc_new_currents(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt
 int ckt_calc_new_currents_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                               const ckt_params *prm, void *stream) {
   int rc;
-  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
-      (rc = check_graph_wires(graph, wires)))
-    return rc;
+  CKT_REQUIRE(graph != nullptr, "graph is NULL");
+  if ((rc = validate_params(prm))) return rc;
+  if (graph->W == 0) return CKT_OK;
+  if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.voltage != nullptr, "node voltage array is NULL");
   return launch_cnc(0, (uint32_t)graph->W, wires, nodes.voltage, nodes.voltage, nodes.voltage, prm,
                     as_stream(stream));
@@ -136,9 +149,12 @@ int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires
                           ckt_nodes pvt, float *shr_fold, float *ghost_fold,
                           const ckt_params *prm, void *stream) {
   int rc;
-  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
-      (rc = check_graph_wires(graph, wires)))
-    return rc;
+  CKT_REQUIRE(graph != nullptr, "graph is NULL");
+  if ((rc = validate_params(prm))) return rc;
+  CKT_REQUIRE(piece_index >= 0 && piece_index < graph->P, "piece_index %d out of range [0, %d)",
+              piece_index, graph->P);
+  if (graph->pieces[piece_index].num_wires == 0) return CKT_OK;
+  if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(piece_index >= 0 && piece_index < graph->P, "piece_index %d out of range [0, %d)",
               piece_index, graph->P);
   CKT_REQUIRE(pvt.charge != nullptr, "pvt.charge is NULL");
@@ -171,14 +187,14 @@ int ckt_apply_fold(const ckt_graph *graph, int32_t piece_index, float *shr_fold,
 int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                               const ckt_params *prm, void *stream) {
   int rc;
-  if ((rc = validate_wires(wires)) || (rc = validate_params(prm)) ||
-      (rc = check_graph_wires(graph, wires)))
-    return rc;
+  CKT_REQUIRE(graph != nullptr, "graph is NULL");
+  if ((rc = validate_params(prm))) return rc;
+  if (graph->N == 0 || graph->W == 0) return CKT_OK;  // no wire deposits anything
+  if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
-  if (graph->N == 0) return CKT_OK;
   const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
-  dc_all_kernel<<<grid_for(graph->N), 256, 0, as_stream(stream)>>>(
-      (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, prm->dt);
+  dc_all_kernel<<<grid_for(graph->N, kDcBlock), kDcBlock, 0, as_stream(stream)>>>(
+      0u, (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, prm->dt);
   CKT_CHECK_LAUNCH();
   return CKT_OK;
 }

@@ -126,7 +126,7 @@ def test_per_piece_calls_equal_index_space(cuda, oracle, shape):
         assert same_bits(a[k], getattr(c, k)), k
 
 
-@pytest.mark.parametrize("steps,loops", [(1, 1), (2, 1), (4, 2), (6, 3)])
+@pytest.mark.parametrize("steps,loops", [(1, 1), (2, 1), (3, 2), (4, 2), (6, 1)])
 def test_fast_mode_within_tolerance(cuda, oracle, steps, loops):
     c = oracle.generate(oracle.GenParams(4, 256, 1024, 95, 12345, L_offset=0.001))
     c64 = c.astype(np.float64)
@@ -135,6 +135,7 @@ def test_fast_mode_within_tolerance(cuda, oracle, steps, loops):
     oracle.simulate(c64, loops, steps)
     for k in STATE:
         ref = getattr(c, k)
+        assert np.isfinite(ref).all(), "case left the finite regime"
         assert np.array_equal(np.isfinite(got[k]), np.isfinite(ref)), k
         r = np.abs(got[k].astype(np.float64) - ref) / np.maximum(np.abs(ref), FAST_TINY)
         assert r.max() <= FAST_RTOL, (k, r.max())
