@@ -175,6 +175,27 @@ int ckt_update_voltages(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
 int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num_nodes_total,
                            int64_t *first_bad, void *stream);
 
+/* Allocation-free wire check.  No counterpart in the reference.
+ * Checks pieces[0..num_pieces) in one launch, giving for each piece what
+ * ckt_sanity_check_wires gives for it (first_bad[k]: smallest failing wire
+ * of piece k, or -1), but allocates nothing -- neither device nor host
+ * memory.  For callers that cannot allocate: a runtime that reserves the
+ * GPU's memory for its own pools at start-up, code that must not call
+ * cudaMalloc/cudaFree because they can synchronise the device, a process
+ * held to a fixed memory budget.  Its scratch is one fixed array of
+ * CKT_NOALLOC_MAX_PIECES slots (24 bytes each, 96 KB) that every GPU loading
+ * the library holds until the process exits.
+ *  - num_pieces above CKT_NOALLOC_MAX_PIECES is rejected with CKT_EINVAL.
+ *  - The first call on a device looks up the array's device address (with
+ *    that device current); make that first call before any stream capture.
+ *  - Every call uses the same array and leaves its contents behind (each
+ *    call re-initialises what it reads).  Calls that overlap on the GPU --
+ *    other streams, other host threads -- race on it: serialise them.
+ *  - Synchronises `stream`; returns CKT_EBOUNDS when any piece fails. */
+#define CKT_NOALLOC_MAX_PIECES 4096
+int ckt_sanity_check_pieces_noalloc(const ckt_piece *pieces, int32_t num_pieces, ckt_wires wires,
+                                    uint32_t num_nodes_total, int64_t *first_bad, void *stream);
+
 /* ------------------------------------------------------------------------
  * Index-space launches: one launch per task over all pieces of a circuit
  * (the three execute_index_space calls of apps/circuit/circuit.cc:250-298),

@@ -97,6 +97,8 @@ SIGNATURES = {
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
     "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _P, _P]),
+    "ckt_sanity_check_pieces_noalloc": (ctypes.c_int, [ctypes.POINTER(Piece), _I32, Wires, _U32,
+                                                       ctypes.POINTER(_I64), _P]),
     "ckt_batch_create": (ctypes.c_int, [_I32, ctypes.POINTER(GenParams),
                                         ctypes.POINTER(HostCircuit), ctypes.POINTER(_I32),
                                         ctypes.POINTER(_P)]),
