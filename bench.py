@@ -200,22 +200,28 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def fp32_peak(torch, G, stream) -> float:
-    """Measured FP32 FMA throughput (FLOP/s) of this GPU (best of 5)."""
+def fp32_peak(torch, G, stream) -> dict:
+    """Measured FP32 FMA throughput (FLOP/s) of this GPU, best of 5, with
+    single and with paired (f32x2) FMAs; the roofline uses the larger."""
     sm = torch.cuda.get_device_properties(0).multi_processor_count
     sink = torch.zeros(1, device="cuda")
     blocks, iters = sm * 8, 2048
     flops = blocks * 256 * iters * 16 * 8 * 2
-    best = 0.0
+    out = {}
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for i in range(6):
-        s0.record(stream)
-        G.check(G.lib().ckt_fp32_fma_probe(blocks, iters, sink.data_ptr(), stream.cuda_stream))
-        s1.record(stream)
-        s1.synchronize()
-        if i:
-            best = max(best, flops / (s0.elapsed_time(s1) * 1e-3))
-    return best
+    for paired in (0, 1):
+        best = 0.0
+        for i in range(6):
+            s0.record(stream)
+            G.check(G.lib().ckt_fp32_fma_probe(blocks, iters, paired, sink.data_ptr(),
+                                               stream.cuda_stream))
+            s1.record(stream)
+            s1.synchronize()
+            if i:
+                best = max(best, flops / (s0.elapsed_time(s1) * 1e-3))
+        out["paired" if paired else "single"] = best
+    out["peak"] = max(out["single"], out["paired"])
+    return out
 
 
 def main() -> None:
@@ -228,6 +234,8 @@ def main() -> None:
     ap.add_argument("--cpu-sample-s", type=float, default=3.0,
                     help="target seconds of CPU work per sampled step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["plain", "batched"], default="plain",
+                    help="plain: 64x16384x65536 circuit (default); batched: 256 mixed circuits")
     ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
                     help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
     args = ap.parse_args()
@@ -255,6 +263,10 @@ def main() -> None:
     B.build()
     L = G.lib()
     mode = G.MODE_FAST if args.mode == "fast" else G.MODE_EXACT
+
+    if args.workload == "batched":
+        run_batched(args, torch, G, ws, rank, local, dist, mode)
+        return
 
     # CPU baseline first (rank 0, N=1 only), before any GPU work is queued.
     cpu_baseline = None
@@ -335,7 +347,8 @@ def main() -> None:
     kt = {k: [a.elapsed_time(b) * 1e-3 for a, b in v] for k, v in kernel_events.items()}
 
     # Roofline of the dominant kernel (calc_new_currents, FP32-pipe bound).
-    peak32 = fp32_peak(torch, G, stream)
+    probe = fp32_peak(torch, G, stream)
+    peak32 = probe["peak"]
     cnc_s = statistics.mean(kt["cnc"])
     cnc_flops = FLOPS_PER_WIRE_STEP * shape.W * INNER_STEPS
     peaks = measured_peaks()
@@ -349,7 +362,9 @@ def main() -> None:
         "kernel": "calc_new_currents", "bound": "fp32", "unit": "TFLOP/s",
         "achieved": cnc_flops / cnc_s / 1e12, "peak": peak32 / 1e12,
         "frac": cnc_flops / cnc_s / peak32,
-        "peak_source": "measured FP32 FMA throughput (ckt_fp32_fma_probe) on this GPU",
+        "peak_source": "measured FP32 FMA throughput on this GPU (ckt_fp32_fma_probe, max of "
+                       f"single {probe['single'] / 1e12:.1f} and paired f32x2 "
+                       f"{probe['paired'] / 1e12:.1f} TFLOP/s)",
         "algorithmic": f"{FLOPS_PER_WIRE_STEP} flops per wire-step x {shape.W} wires x "
                        f"{INNER_STEPS} steps per launch",
         "traffic": None,
@@ -415,6 +430,152 @@ def main() -> None:
             "replicas": "one independent circuit per GPU" if ws > 1 else None,
         }
         print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
+    """Batched mixed sizes: 256 independent circuits (pieces U{1..32}, nodes
+    per piece log-uniform [256, 16384], 4 wires per node, in-piece fraction
+    U[0.8, 0.98], inner steps U{100..1000}, seeds 0..255, one outer loop).
+    One step = reset the batch's state, then one persistent launch (CUDA
+    graph replay) that runs every circuit's loop.  The plain path on the same
+    circuits (circuit after circuit, three launches each) is timed beside it."""
+    from legionorigins_gb300.batch import Batch
+    from legionorigins_gb300.workloads import mixed_batch
+
+    specs = mixed_batch(256)
+    t_build = time.perf_counter()
+    b = Batch(specs, threads=cpu_threads())
+    t_build = time.perf_counter() - t_build
+    info = b.info()
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    cfg = b.autotune(mode, sp)
+    updates = info["segment_updates_per_run"]
+    E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(fn, steps):
+        events = []
+        for _ in range(steps):
+            G.check(G.lib().ckt_batch_reset_state(b.handle, sp))
+            a, z = E(), E()
+            a.record(stream)
+            fn()
+            z.record(stream)
+            events.append((a, z))
+        return events
+
+    for _ in range(args.warmup):
+        b.reset_state(sp)
+        b.run(mode, sp)
+    assert b.check(sp) == 0
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    t0, t1 = E(), E()
+    with Clocks(local) as clk:
+        t0.record(stream)
+        ev = timed(lambda: b.run(mode, sp), args.steps)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if b.check(sp) != 0:
+        raise SystemExit("persistent kernel reported a timeout")
+    elapsed = t0.elapsed_time(t1) * 1e-3
+    if dist is not None:
+        dist.barrier()
+        tt = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    kern = [a.elapsed_time(z) * 1e-3 for a, z in ev]
+    value = ws * updates * args.steps / elapsed
+
+    # The plain path on the same 256 circuits: circuit after circuit with
+    # index-space launches, and piece by piece with a synchronisation after
+    # every launch (the reference's task granularity).  Wall-clock timed.
+    def plain(per_piece):
+        b.reset_state(sp)
+        b.run_sequential(mode, sp, per_piece)
+        torch.cuda.synchronize()
+        steps_ = max(1, min(args.steps, 3))
+        w0 = time.perf_counter()
+        for _ in range(steps_):
+            G.check(G.lib().ckt_batch_reset_state(b.handle, sp))
+            b.run_sequential(mode, sp, per_piece)
+        torch.cuda.synchronize()
+        return updates * steps_ / (time.perf_counter() - w0)
+
+    seq = plain(False)
+    seq_piece = plain(True)
+    pieces_total = sum(s.num_pieces for s in specs)
+
+    # End to end: every step copies the batch's state in from pinned host
+    # memory, runs, and copies it back (topology and constants stay resident).
+    W, N = info["wires"], info["nodes"]
+    hin = [torch.zeros(n, dtype=torch.float32).pin_memory() for n in (10 * W, 9 * W, N, N)]
+    G.check(G.lib().ckt_batch_reset_state(b.handle, sp))
+    G.check(G.lib().ckt_batch_download_state(b.handle, *[t.data_ptr() for t in hin], sp))
+    hout = [torch.empty_like(t).pin_memory() for t in hin]
+    torch.cuda.synchronize()
+    h2d = sum(t.numel() * 4 for t in hin)
+
+    def e2e_step():
+        G.check(G.lib().ckt_batch_upload_state(b.handle, *[t.data_ptr() for t in hin], sp))
+        b.run(mode, sp)
+        G.check(G.lib().ckt_batch_download_state(b.handle, *[t.data_ptr() for t in hout], sp))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = E(), E()
+    w0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = max(e0.elapsed_time(e1) * 1e-3, time.perf_counter() - w0)
+
+    probe = fp32_peak(torch, G, stream)
+    flops = sum(FLOPS_PER_WIRE_STEP * s.wires * s.steps for s in specs)
+    k_mean = statistics.mean(kern)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (reference generator distributions, seeds 0..255)",
+            "config": {
+                "workload": "batched mixed sizes: 256 independent circuits, pieces U{1..32}, "
+                            "nodes/piece log-uniform [256,16384], 4 wires/node, in-piece "
+                            "U[0.8,0.98], inner steps U{100..1000}, 1 outer loop; one "
+                            "persistent launch per step (CUDA graph)",
+                "mode": args.mode, "circuits": len(specs), "wires": sum(s.wires for s in specs),
+                "segment_updates_per_step": updates, "launch_shape": cfg,
+                "l2": f"inputs larger than L2 ({19 * W * 4 / 1e9:.1f} GB of wire state)",
+                "host_build_s": t_build,
+            },
+            "plain_sequential": {
+                "index_space_per_circuit": {"value": seq, "unit": UNIT,
+                                            "speedup_batched_over_it": value / seq,
+                                            "launches_per_step": 4 * len(specs)},
+                "per_piece_synchronous": {"value": seq_piece, "unit": UNIT,
+                                          "speedup_batched_over_it": value / seq_piece,
+                                          "launches_per_step": 2 * pieces_total + 2 * len(specs)},
+            },
+            "roofline": {"kernel": "batch_kernel (persistent: calc_new_currents + "
+                                   "distribute_charge + update_voltages)",
+                         "bound": "fp32", "unit": "TFLOP/s", "achieved": flops / k_mean / 1e12,
+                         "peak": probe["peak"] / 1e12, "frac": flops / k_mean / probe["peak"],
+                         "traffic": None},
+            "cpu_baseline": None,
+            "e2e": {"value": ws * updates * args.steps / e2e_s, "unit": UNIT,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "note": "circuit state in and out every step; topology resident"},
+            "gpu_launches": args.steps, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -54,8 +54,12 @@ typedef enum {
    * divides, no contraction): bit-identical to the reference CPU task. */
   CKT_MODE_EXACT = 0,
   /* Loop-invariant quotients L/dt, 1/R and dt/C hoisted out of the inner
-   * loop and fused multiply-adds: within 1e-5 relative of EXACT. */
-  CKT_MODE_FAST = 1
+   * loop and fused multiply-adds: within 1e-5 relative of EXACT.  Issued as
+   * paired FP32 instructions (two segments per instruction). */
+  CKT_MODE_FAST = 1,
+  /* FAST arithmetic issued one segment per instruction: bit-identical to
+   * CKT_MODE_FAST (kept to check the paired form and to measure it). */
+  CKT_MODE_FAST_SCALAR = 2
 } ckt_mode;
 
 /* Wire initialisation of calc_new_currents. */
@@ -267,7 +271,9 @@ typedef struct ckt_batch ckt_batch;
 typedef struct {
   int32_t block;            /* threads per block: 128 or 256 */
   int32_t wires_per_thread; /* calc_new_currents wires per thread per tile: 1 or 2 */
-  int32_t dc_schedule;      /* distribute_charge: 0 staged block gather, 1 thread per node */
+  int32_t dc_schedule;      /* distribute_charge: 0 staged block gather, 1 thread per node,
+                               2 contributions scattered by the calc_new_currents tiles, then
+                               summed contiguously */
   int32_t blocks_per_sm;    /* output: resident blocks per SM of the persistent grid */
 } ckt_batch_config;
 
@@ -296,9 +302,12 @@ int ckt_batch_autotune(ckt_batch *batch, int32_t mode, void *stream, ckt_batch_c
 int ckt_batch_run(ckt_batch *batch, int32_t mode, void *stream);
 /* Same launch without the graph. */
 int ckt_batch_run_direct(ckt_batch *batch, int32_t mode, void *stream);
-/* The plain path on the same batch: circuit after circuit, three launches
- * each (the comparison point of the batched form). */
-int ckt_batch_run_sequential(ckt_batch *batch, int32_t mode, void *stream);
+/* The plain path on the same batch, circuit after circuit (the comparison
+ * point of the batched form): per_piece = 0, one launch per task per circuit
+ * (index-space calls); per_piece = 1, calc_new_currents and update_voltages
+ * launched piece by piece with a stream synchronisation after each launch,
+ * as the reference's GPU task wrappers do (circuit_gpu.cu:204,367). */
+int ckt_batch_run_sequential(ckt_batch *batch, int32_t mode, int32_t per_piece, void *stream);
 /* Synchronises `stream` and reads the persistent kernel's error word:
  * CKT_ETIMEOUT if a bounded wait ran out. */
 int ckt_batch_check(ckt_batch *batch, void *stream);
@@ -310,8 +319,12 @@ int ckt_batch_reset_state(ckt_batch *batch, void *stream);
  * [N_i]); NULL skips a field.  Synchronous. */
 int ckt_batch_read_state(ckt_batch *batch, int32_t circuit, float *current, float *voltage,
                          float *charge, float *node_voltage, void *stream);
-/* Whole-union state from / to host memory (sizes from ckt_batch_info;
- * asynchronous on `stream`; pinned host memory gives full copy speed). */
+/* The whole batch's state from / to host memory, asynchronous on `stream`
+ * (pinned host memory gives full copy speed).  Layout: circuit blocks back
+ * to back in circuit order -- current[10 * W_total] holds circuit i's
+ * [10][W_i] block at 10 * first_wire(i), voltage likewise with 9, charge and
+ * node_voltage [N_total] hold circuit i's nodes at first_node(i) (node
+ * blocks padded to multiples of 4); see ckt_batch_circuit_offsets. */
 int ckt_batch_upload_state(ckt_batch *batch, const float *current, const float *voltage,
                            const float *charge, const float *node_voltage, void *stream);
 int ckt_batch_download_state(ckt_batch *batch, float *current, float *voltage, float *charge,
@@ -323,11 +336,13 @@ int ckt_batch_inject_stall(ckt_batch *batch, int32_t circuit, int32_t enable);
 
 /* ------------------------------------------------------------------------
  * Measurement helper (no counterpart in the reference): FP32 FMA throughput
- * probe.  Launches `blocks` x 256 threads, each issuing iters*16*8
- * independent fused multiply-adds (2 flops each); time it on `stream` to
- * get the device's FP32-pipe peak.  `sink` is a device float it may write.
+ * probe.  Launches `blocks` x 256 threads, each performing iters*16*8
+ * independent fused multiply-adds (2 flops each) -- as single FMAs, or with
+ * `paired` != 0 as paired (f32x2) FMAs doing two each; time it on `stream`
+ * to get the device's FP32-pipe peak.  `sink` is a device float it may
+ * write.
  * ---------------------------------------------------------------------- */
-int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, float *sink, void *stream);
+int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, int32_t paired, float *sink, void *stream);
 
 #ifdef __cplusplus
 }

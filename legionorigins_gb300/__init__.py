@@ -18,7 +18,7 @@ __all__ = ["lib", "CktError", "Piece", "Wires", "Nodes", "Params", "GenParams", 
 
 LIB_PATH = _build.LIB
 
-MODE_EXACT, MODE_FAST = 0, 1
+MODE_EXACT, MODE_FAST, MODE_FAST_SCALAR = 0, 1, 2
 INIT_KERNEL, INIT_CPU_TASK = 0, 1
 PRIVATE_PTR, SHARED_PTR, GHOST_PTR = 0, 1, 2
 SEGMENTS = 10
@@ -96,7 +96,7 @@ SIGNATURES = {
     "ckt_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
-    "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _P, _P]),
+    "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
     "ckt_sanity_check_pieces_noalloc": (ctypes.c_int, [ctypes.POINTER(Piece), _I32, Wires, _U32,
                                                        ctypes.POINTER(_I64), _P]),
     "ckt_batch_create": (ctypes.c_int, [_I32, ctypes.POINTER(GenParams),
@@ -114,7 +114,7 @@ SIGNATURES = {
     "ckt_batch_autotune": (ctypes.c_int, [_P, _I32, _P, ctypes.POINTER(BatchConfig)]),
     "ckt_batch_run": (ctypes.c_int, [_P, _I32, _P]),
     "ckt_batch_run_direct": (ctypes.c_int, [_P, _I32, _P]),
-    "ckt_batch_run_sequential": (ctypes.c_int, [_P, _I32, _P]),
+    "ckt_batch_run_sequential": (ctypes.c_int, [_P, _I32, _I32, _P]),
     "ckt_batch_check": (ctypes.c_int, [_P, _P]),
     "ckt_batch_set_timeout": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "ckt_batch_reset_state": (ctypes.c_int, [_P, _P]),

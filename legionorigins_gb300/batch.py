@@ -69,8 +69,8 @@ class Batch:
     def run_direct(self, mode: int, stream: int = 0) -> None:
         check(lib().ckt_batch_run_direct(self.handle, mode, stream))
 
-    def run_sequential(self, mode: int, stream: int = 0) -> None:
-        check(lib().ckt_batch_run_sequential(self.handle, mode, stream))
+    def run_sequential(self, mode: int, stream: int = 0, per_piece: bool = False) -> None:
+        check(lib().ckt_batch_run_sequential(self.handle, mode, int(per_piece), stream))
 
     def check(self, stream: int = 0) -> int:
         """0, or the ckt_status of the last run (e.g. 4 = a wait timed out)."""

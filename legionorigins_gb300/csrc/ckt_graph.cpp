@@ -38,6 +38,10 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->touch_loc);
   cudaFree(g->touch_off);
   cudaFree(g->piece_ent);
+  cudaFree(g->slot_in);
+  cudaFree(g->slot_out);
+  cudaFree(g->gstart);
+  cudaFree(g->contrib);
   delete g;
 }
 
@@ -50,7 +54,7 @@ namespace ckt {
 int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
                    const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
                    const uint8_t *out_loc, std::vector<uint32_t> &off, std::vector<uint32_t> &ent,
-                   int64_t *num_wires) {
+                   int64_t *num_wires, std::vector<uint32_t> *slots) {
   CKT_REQUIRE(num_pieces >= 1 && pieces != nullptr, "need at least one piece");
   // Pieces tile [0, W) in order; node ranges lie inside [0, N) and are disjoint.
   int64_t W = 0;
@@ -115,6 +119,7 @@ int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nod
   {
     std::vector<uint32_t> fill(off.begin(), off.end() - 1);
     std::vector<int32_t> last_piece(N, -1);
+    if (slots) slots->assign(2 * W, 0);
     for (int32_t k = 0; k < num_pieces; k++) {
       const ckt_piece &p = pieces[k];
       for (int64_t w = p.first_wire; w < (int64_t)p.first_wire + p.num_wires; w++) {
@@ -123,6 +128,7 @@ int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nod
           const uint32_t x = xs[e];
           const uint32_t start = last_piece[x] != k ? 1u : 0u;
           last_piece[x] = k;
+          if (slots) (*slots)[2 * w + e] = fill[x];
           ent[fill[x]++] = ((uint32_t)w << 2) | (e << 1) | start;
         }
       }
@@ -143,11 +149,18 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
                      const uint8_t *out_loc, ckt_graph **out) {
   CKT_REQUIRE(out != nullptr, "out is NULL");
   *out = nullptr;
-  std::vector<uint32_t> off, ent;
+  std::vector<uint32_t> off, ent, slots;
   int64_t W = 0;
   int rc = build_node_csr(pieces, num_pieces, num_nodes, in_ptr, out_ptr, in_loc, out_loc, off,
-                          ent, &W);
+                          ent, &W, &slots);
   if (rc) return rc;
+  std::vector<uint32_t> slot_in(W), slot_out(W), gstart((2 * W + 31) / 32, 0u);
+  for (int64_t w = 0; w < W; w++) {
+    slot_in[w] = slots[2 * w];
+    slot_out[w] = slots[2 * w + 1];
+  }
+  for (int64_t i = 0; i < 2 * W; i++)
+    if (ent[i] & 1u) gstart[i >> 5] |= 1u << (i & 31);
 
   ckt_graph *g = new ckt_graph();
   g->W = W;
@@ -191,7 +204,11 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
       (rc = upload(&g->touch_node, touch_node, &g->device_bytes)) ||
       (rc = upload(&g->touch_loc, touch_loc, &g->device_bytes)) ||
       (rc = upload(&g->touch_off, touch_off, &g->device_bytes)) ||
-      (rc = upload(&g->piece_ent, pent, &g->device_bytes))) {
+      (rc = upload(&g->piece_ent, pent, &g->device_bytes)) ||
+      (rc = upload(&g->slot_in, slot_in, &g->device_bytes)) ||
+      (rc = upload(&g->slot_out, slot_out, &g->device_bytes)) ||
+      (rc = upload(&g->gstart, gstart, &g->device_bytes)) ||
+      (rc = upload(&g->contrib, std::vector<float>(2 * W), &g->device_bytes))) {
     free_graph(g);
     return rc;
   }

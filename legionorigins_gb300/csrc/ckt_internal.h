@@ -53,10 +53,12 @@ inline unsigned grid_for(uint64_t n, unsigned block = 256) {
 
 // Validates the wires against the pieces and builds the whole-circuit CSR
 // (node offsets with the private bit, entries in reduction order).
+// When slots is non-null it also receives, per wire, the CSR positions of
+// its in-end and out-end ([2W]: in at 2w, out at 2w+1).
 int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nodes,
                    const uint32_t *in_ptr, const uint32_t *out_ptr, const uint8_t *in_loc,
                    const uint8_t *out_loc, std::vector<uint32_t> &off, std::vector<uint32_t> &ent,
-                   int64_t *num_wires);
+                   int64_t *num_wires, std::vector<uint32_t> *slots = nullptr);
 
 // calc_new_currents over wires [first, first + n) (any mode/initialisation).
 int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp, const float *vs,
@@ -84,5 +86,10 @@ struct ckt_graph {
   uint8_t *touch_loc = nullptr;      // [T]
   uint32_t *touch_off = nullptr;     // [T + 1] into piece_ent
   uint32_t *piece_ent = nullptr;     // [2W]
+  // Two-pass distribute_charge: each wire end's CSR position, a bit per CSR
+  // entry marking the start of a piece group, and the contribution buffer.
+  uint32_t *slot_in = nullptr, *slot_out = nullptr;  // [W]
+  uint32_t *gstart = nullptr;                        // [ceil(2W / 32)]
+  float *contrib = nullptr;                          // [2W] scratch
   int64_t device_bytes = 0;
 };

@@ -37,7 +37,9 @@ int validate_nodes(const ckt_nodes &n, const char *what) {
 int validate_params(const ckt_params *p) {
   CKT_REQUIRE(p != nullptr, "params is NULL");
   CKT_REQUIRE(p->steps >= 0, "steps must be >= 0 (got %d)", p->steps);
-  CKT_REQUIRE(p->mode == CKT_MODE_EXACT || p->mode == CKT_MODE_FAST, "unknown mode %d", p->mode);
+  CKT_REQUIRE(p->mode == CKT_MODE_EXACT || p->mode == CKT_MODE_FAST ||
+                  p->mode == CKT_MODE_FAST_SCALAR,
+              "unknown mode %d", p->mode);
   CKT_REQUIRE(p->init == CKT_INIT_KERNEL || p->init == CKT_INIT_CPU_TASK, "unknown init %d", p->init);
   return CKT_OK;
 }
@@ -74,9 +76,12 @@ int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
   if (p->mode == CKT_MODE_EXACT) {
     if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_EXACT, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
     else launch_cnc_t<CKT_MODE_EXACT, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
-  } else {
+  } else if (p->mode == CKT_MODE_FAST) {
     if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_FAST, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
     else launch_cnc_t<CKT_MODE_FAST, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
+  } else {
+    if (p->init == CKT_INIT_KERNEL) launch_cnc_t<kModeFastScalar, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
+    else launch_cnc_t<kModeFastScalar, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
   }
   CKT_CHECK_LAUNCH();
   return CKT_OK;
@@ -193,8 +198,13 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
   const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
-  dc_all_kernel<<<grid_for(graph->N, kDcBlock), kDcBlock, 0, as_stream(stream)>>>(
-      0u, (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, prm->dt);
+  const cudaStream_t s = as_stream(stream);
+  dc_scatter_kernel<<<grid_for(graph->W), 256, 0, s>>>((uint32_t)graph->W, graph->slot_in,
+                                                       graph->slot_out, I0, I9, graph->contrib,
+                                                       prm->dt);
+  CKT_CHECK_LAUNCH();
+  dc_sum_kernel<<<grid_for(graph->N), 256, 0, s>>>(0u, (uint32_t)graph->N, graph->node_off,
+                                                   graph->contrib, graph->gstart, nodes.charge);
   CKT_CHECK_LAUNCH();
   return CKT_OK;
 }

@@ -73,16 +73,17 @@ def test_every_launch_shape_and_the_sequential_path_agree(cuda, specs):
     results = []
     for block in (128, 256):
         for wpt in (1, 2):
-            for dcs in (0, 1):
+            for dcs in (0, 1, 2):
                 b.set_config(block, wpt, dcs)
                 b.reset_state()
                 b.run(0)
                 assert b.check() == 0
                 results.append([b.read(i) for i in range(len(specs))])
-    b.reset_state()
-    b.run_sequential(0)
-    cuda.cuda.synchronize()
-    results.append([b.read(i) for i in range(len(specs))])
+    for per_piece in (False, True):
+        b.reset_state()
+        b.run_sequential(0, per_piece=per_piece)
+        cuda.cuda.synchronize()
+        results.append([b.read(i) for i in range(len(specs))])
     for r in results[1:]:
         for i in range(len(specs)):
             for k in STATE:

@@ -144,6 +144,21 @@ def test_fast_mode_within_tolerance(cuda, oracle, steps, loops):
               f"vs fp64 max {e64.max():.2e} rms {np.sqrt((e64 ** 2).mean()):.2e}")
 
 
+@pytest.mark.parametrize("steps,loops", [(1, 1), (3, 2), (1000, 2)])
+@pytest.mark.parametrize("init", [0, 1])
+def test_paired_fast_equals_scalar_fast(cuda, oracle, steps, loops, init):
+    """The paired-instruction FAST step rounds every segment exactly as the
+    one-at-a-time FAST step: identical bits."""
+    c = oracle.generate(oracle.GenParams(4, 256, 1024, 95, 12345, L_offset=0.001))
+    rng = np.random.default_rng(7)
+    c.current[:] = rng.uniform(-1, 1, c.current.shape).astype(np.float32)
+    c.voltage[:] = rng.uniform(-1, 1, c.voltage.shape).astype(np.float32)
+    a = run_gpu(cuda, device(cuda, c), loops, steps, mode=1, init=init)
+    b = run_gpu(cuda, device(cuda, c), loops, steps, mode=2, init=init)
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+
+
 def test_fast_mode_classes_at_configured_steps(cuda, oracle):
     c = oracle.generate(oracle.GenParams(4, 256, 1024, 95, 12345, L_offset=0.001))
     got = run_gpu(cuda, device(cuda, c), 5, 1000, mode=1)
