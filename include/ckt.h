@@ -213,6 +213,22 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
 int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Reference-instance interop: conversion between the reference's
+ * array-of-structs instances -- CircuitWire (128 bytes: in_ptr, out_ptr,
+ * in_loc, out_loc as 4-byte ints, inductance, resistance, current[10],
+ * capacitance, voltage[9], 6 pad floats) and CircuitNode (16 bytes: charge,
+ * voltage, capacitance, leakage), apps/circuit/circuit.h:35-54 -- and the
+ * structure-of-arrays views.  The AoS pointer may be device memory or host
+ * memory mapped for the device (zero-copy instances, the placement of
+ * apps/circuit/circuit.cc:903-914); it must be 16-byte aligned.  Pad floats
+ * are written as zero.  Asynchronous on `stream`.
+ * ---------------------------------------------------------------------- */
+int ckt_wires_from_aos(const void *aos, int64_t num_wires, ckt_wires soa, void *stream);
+int ckt_wires_to_aos(ckt_wires soa, int64_t num_wires, void *aos, void *stream);
+int ckt_nodes_from_aos(const void *aos, int64_t num_nodes, ckt_nodes soa, void *stream);
+int ckt_nodes_to_aos(ckt_nodes soa, int64_t num_nodes, void *aos, void *stream);
+
+/* ------------------------------------------------------------------------
  * Contribution graph
  * ---------------------------------------------------------------------- */
 
@@ -255,6 +271,36 @@ typedef struct {
 } ckt_host_circuit;
 
 int ckt_generate(const ckt_gen_params *p, ckt_host_circuit *out);
+
+/* Device-resident circuit with its contribution graph (all device
+ * pointers, caller-allocated): wire arrays [W] (current [10][W], voltage
+ * [9][W], ent [2W], gstart [ceil(2W/32)]), node arrays [N], off [N + 1]. */
+typedef struct {
+  uint32_t *in_ptr, *out_ptr;
+  uint8_t *in_loc, *out_loc;
+  float *inductance, *resistance, *capacitance;
+  float *current, *voltage;
+  float *charge, *node_voltage, *node_capacitance, *node_leakage;
+  int32_t *locator;
+  uint32_t *off;       /* node CSR offsets; bit 31 = private node */
+  uint32_t *ent;       /* (wire << 2) | (end << 1) | starts-new-piece-group */
+  uint32_t *slot_in;   /* CSR position of each wire's in-end */
+  uint32_t *slot_out;  /* CSR position of each wire's out-end */
+  uint32_t *gstart;    /* bit i = entry i starts a piece group */
+} ckt_device_circuit;
+
+/* The generator on the GPU: the same drand48 stream, graph and initial
+ * values as ckt_generate, bit for bit, written straight into device memory,
+ * and the contribution graph built there too (identical to the one
+ * ckt_graph_create builds from the same wires).  Asynchronous on `stream`;
+ * uses stream-ordered scratch memory. */
+int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *out, void *stream);
+
+/* Copies a graph's whole-circuit CSR to host arrays (off [N + 1], ent [2W],
+ * slot_in [W], slot_out [W], gstart [ceil(2W/32)]); NULL skips a field. */
+int ckt_graph_export(const ckt_graph *graph, uint32_t *off, uint32_t *ent, uint32_t *slot_in,
+                     uint32_t *slot_out, uint32_t *gstart);
+
 
 /* ------------------------------------------------------------------------
  * Batched form: many independent circuits of uneven sizes.  One call of
@@ -333,6 +379,77 @@ int ckt_batch_download_state(ckt_batch *batch, float *current, float *voltage, f
  * tiles wait for a calc_new_currents tile that does not exist, so the wait
  * runs out (enable = 0 restores the table). */
 int ckt_batch_inject_stall(ckt_batch *batch, int32_t circuit, int32_t enable);
+
+/* ------------------------------------------------------------------------
+ * Serving loop: circuit-solve requests arrive over time; each is built,
+ * admitted when a slot and the HBM budget allow, kept resident on the
+ * device, and advanced one outer loop per "round" -- one persistent launch
+ * over every resident circuit -- until its loops are done (continuous
+ * batching: requests join and leave between rounds; uploads and downloads
+ * overlap the rounds).  Results are bit-identical to running the request
+ * alone.  No counterpart in the reference.
+ * ---------------------------------------------------------------------- */
+typedef struct ckt_server ckt_server;
+
+typedef struct {
+  uint64_t hbm_budget_bytes; /* admission budget for resident circuits */
+  int32_t max_circuits;      /* resident circuit slots */
+  int32_t prep_threads;      /* host threads building requests' circuits */
+  int32_t mode;              /* CKT_MODE_EXACT or CKT_MODE_FAST */
+  int32_t keep_results;      /* keep final state for ckt_server_take_result */
+  uint64_t round_timeout_ns; /* bound of the round kernel's device waits */
+  ckt_batch_config launch;   /* round kernel launch shape */
+  int32_t device_generate;   /* 1: build circuits with ckt_generate_device on the GPU;
+                                0: on the host (prep_threads) and upload them */
+  int32_t reserved;
+} ckt_server_config;
+
+/* One request: a circuit from the reference generator (shape and seed),
+ * `steps` inner steps, `loops` outer loops. */
+typedef struct {
+  uint64_t request_id;
+  ckt_gen_params shape;
+  int32_t steps;
+  int32_t loops;
+} ckt_request;
+
+/* Times are seconds on the server's clock (ckt_server_clock). */
+typedef struct {
+  uint64_t request_id;
+  int32_t status; /* CKT_OK, CKT_ENOMEM (larger than the budget),
+                     CKT_ECANCELLED, CKT_ETIMEOUT, CKT_EBOUNDS, ... */
+  int32_t loops;  /* loops completed */
+  double submit_s, admit_s, start_s, finish_s;
+  int64_t wires, nodes;
+  double segment_updates; /* wires x 10 x steps x loops completed */
+} ckt_completion;
+
+typedef struct {
+  int64_t submitted, completed, rounds, resident_peak;
+  uint64_t bytes_in_use, bytes_peak;
+  double busy_s, clock_s;
+} ckt_server_stats;
+
+/* 80 GB budget, 4096 slots, one prep thread per host core, FAST, results
+ * not kept, 5 s round timeout, launch {256, 1, 2}, device generation. */
+void ckt_server_default_config(ckt_server_config *config);
+int ckt_server_create(const ckt_server_config *config, ckt_server **out);
+/* Non-blocking; the id must be unused among the server's open requests. */
+int ckt_server_submit(ckt_server *server, const ckt_request *request);
+int ckt_server_cancel(ckt_server *server, uint64_t request_id);
+/* Up to `capacity` finished requests, oldest first; non-blocking. */
+int ckt_server_poll(ckt_server *server, ckt_completion *out, int32_t capacity, int32_t *count);
+/* Blocks until every submitted request has finished (CKT_ETIMEOUT after
+ * timeout_s). */
+int ckt_server_wait(ckt_server *server, double timeout_s);
+/* With keep_results: copies a finished request's final state ([10][W],
+ * [9][W], [N], [N]) and forgets it. */
+int ckt_server_take_result(ckt_server *server, uint64_t request_id, float *current,
+                           float *voltage, float *charge, float *node_voltage);
+int ckt_server_get_stats(ckt_server *server, ckt_server_stats *out);
+double ckt_server_clock(const ckt_server *server);
+/* Stops the threads, abandons open requests and frees everything. */
+int ckt_server_destroy(ckt_server *server);
 
 /* ------------------------------------------------------------------------
  * Measurement helper (no counterpart in the reference): FP32 FMA throughput

@@ -71,6 +71,41 @@ class BatchConfig(ctypes.Structure):
                 ("dc_schedule", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_circuits", ctypes.c_int32),
+                ("prep_threads", ctypes.c_int32), ("mode", ctypes.c_int32),
+                ("keep_results", ctypes.c_int32), ("round_timeout_ns", ctypes.c_uint64),
+                ("launch", BatchConfig), ("device_generate", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("shape", GenParams), ("steps", ctypes.c_int32),
+                ("loops", ctypes.c_int32)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("status", ctypes.c_int32),
+                ("loops", ctypes.c_int32), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("start_s", ctypes.c_double),
+                ("finish_s", ctypes.c_double), ("wires", ctypes.c_int64),
+                ("nodes", ctypes.c_int64), ("segment_updates", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("rounds", ctypes.c_int64), ("resident_peak", ctypes.c_int64),
+                ("bytes_in_use", ctypes.c_uint64), ("bytes_peak", ctypes.c_uint64),
+                ("busy_s", ctypes.c_double), ("clock_s", ctypes.c_double)]
+
+
+class DeviceCircuitArrays(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "in_ptr", "out_ptr", "in_loc", "out_loc", "inductance", "resistance", "capacitance",
+        "current", "voltage", "charge", "node_voltage", "node_capacitance", "node_leakage",
+        "locator", "off", "ent", "slot_in", "slot_out", "gstart")]
+
+
 # (name, restype, argtypes) of every exported symbol declared in include/ckt.h
 _P = ctypes.c_void_p
 _I32, _I64, _U32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32
@@ -122,6 +157,24 @@ SIGNATURES = {
     "ckt_batch_upload_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "ckt_batch_download_state": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "ckt_batch_inject_stall": (ctypes.c_int, [_P, _I32, _I32]),
+    "ckt_generate_device": (ctypes.c_int, [ctypes.POINTER(GenParams),
+                                           ctypes.POINTER(DeviceCircuitArrays), _P]),
+    "ckt_graph_export": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    "ckt_wires_from_aos": (ctypes.c_int, [_P, _I64, Wires, _P]),
+    "ckt_wires_to_aos": (ctypes.c_int, [Wires, _I64, _P, _P]),
+    "ckt_nodes_from_aos": (ctypes.c_int, [_P, _I64, Nodes, _P]),
+    "ckt_nodes_to_aos": (ctypes.c_int, [Nodes, _I64, _P, _P]),
+    "ckt_server_default_config": (None, [ctypes.POINTER(ServerConfig)]),
+    "ckt_server_create": (ctypes.c_int, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "ckt_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(Request)]),
+    "ckt_server_cancel": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "ckt_server_poll": (ctypes.c_int, [_P, ctypes.POINTER(Completion), _I32,
+                                       ctypes.POINTER(_I32)]),
+    "ckt_server_wait": (ctypes.c_int, [_P, ctypes.c_double]),
+    "ckt_server_take_result": (ctypes.c_int, [_P, ctypes.c_uint64, _P, _P, _P, _P]),
+    "ckt_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    "ckt_server_clock": (ctypes.c_double, [_P]),
+    "ckt_server_destroy": (ctypes.c_int, [_P]),
 }
 
 _lib = None

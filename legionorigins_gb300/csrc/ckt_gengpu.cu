@@ -1,0 +1,422 @@
+// ckt_gengpu.cu -- the circuit generator on the device: the same random
+// stream, graph and initial values as ckt_generate (load_circuit,
+// apps/circuit/circuit.cc:1071-1288), bit for bit, plus the contribution
+// graph of the index-space distribute_charge.
+//
+// drand48 is a 48-bit linear congruential generator, so the state after d
+// draws is A_d*x + C_d (mod 2^48) and any position of the stream can be
+// reached in log2(d) steps.  Nodes draw 3 values each; a wire draws 6 values
+// (in-piece) or 7 (cross-piece), and which one depends on its own 5th draw,
+// so wire start positions are a chain through the stream.  The chain is
+// decoded in parallel by speculation: the stream is cut into chunks of
+// kChunk draws, each chunk is decoded from all 7 possible entry phases (a
+// wire starts at most 6 draws past a chunk boundary), the chunks' phase maps
+// are composed to fix every chunk's true entry phase and first wire index,
+// and every chunk then emits its wires.  Node pointers, locations and the
+// graph follow in data-parallel kernels; per-node contribution lists are
+// sorted by (wire, end) so the graph is identical to the host-built one.
+#include <algorithm>
+#include <vector>
+
+#include "ckt_internal.h"
+
+namespace ckt {
+namespace {
+
+constexpr uint64_t kA = 0x5DEECE66Dull, kC = 0xBull, kMask = 0xffffffffffffull;
+constexpr int kChunk = 1024;     // draws per chunk
+constexpr int kSuper = 64;       // chunks per super-chunk in the map composition
+
+struct Jump {
+  uint64_t a[48], c[48];  // state after 2^i draws: a[i]*x + c[i]
+};
+
+__constant__ Jump g_jump;
+
+Jump make_jump() {
+  Jump j;
+  uint64_t a = kA, c = kC;
+  for (int i = 0; i < 48; i++) {
+    j.a[i] = a;
+    j.c[i] = c;
+    // (a, c) composed with itself: x -> a(ax + c) + c
+    c = (a * c + c) & kMask;
+    a = (a * a) & kMask;
+  }
+  return j;
+}
+
+__device__ __forceinline__ uint64_t skip(uint64_t x, uint64_t d) {
+  for (int i = 0; d; i++, d >>= 1)
+    if (d & 1) x = (g_jump.a[i] * x + g_jump.c[i]) & kMask;
+  return x;
+}
+
+__device__ __forceinline__ double draw(uint64_t &x) {
+  x = (kA * x + kC) & kMask;
+  return (double)x * 0x1p-48;
+}
+
+__device__ __forceinline__ uint32_t pick(double u, uint32_t piece, uint32_t npp) {
+  const int k = (int)(u * (double)npp);
+  return piece * npp + npp - 1 - (uint32_t)k;
+}
+
+struct GenArgs {
+  int32_t P, npp, wpp;
+  double pct, L_off, L_scale;
+  uint64_t seed_state;
+  int64_t W, N;
+};
+
+__device__ __forceinline__ bool crosses(const GenArgs &g, double u5) {
+  return g.P > 1 && !((100 * u5) < g.pct);
+}
+
+// Node values: draws 3x, 3x+1, 3x+2 (circuit.cc:1121-1125).
+__global__ void gen_nodes_kernel(GenArgs g, float *charge, float *nvolt, float *cap, float *leak,
+                                 int32_t *locator) {
+  const int64_t x0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
+  if (x0 >= g.N) return;
+  uint64_t x = skip(g.seed_state, 3 * (uint64_t)x0);
+  const int64_t x1 = min(g.N, x0 + 16);
+  for (int64_t n = x0; n < x1; n++) {
+    charge[n] = 0.f;
+    nvolt[n] = __double2float_rn(__dsub_rn(__dmul_rn(2.0, draw(x)), 1.0));
+    cap[n] = __double2float_rn(__dadd_rn(draw(x), 1.0));
+    leak[n] = __double2float_rn(__dmul_rn((double)0.1f, draw(x)));
+    locator[n] = 1;
+  }
+}
+
+// Per chunk and entry phase q: where the chain leaves the chunk (0..6 past
+// its end) and how many wires start inside it.
+__global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint8_t *exit_phase,
+                                  uint32_t *count) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchunks) return;
+  const int64_t p0 = base + c * kChunk, p1 = p0 + kChunk;
+  uint64_t x = skip(g.seed_state, (uint64_t)p0);
+  int64_t s[7];
+  uint32_t n[7];
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    s[q] = p0 + q;
+    n[q] = 0;
+  }
+  for (int64_t t = p0; t < p1 + 4; t++) {
+    const double u = draw(x);  // draw t
+#pragma unroll
+    for (int q = 0; q < 7; q++)
+      if (s[q] < p1 && s[q] + 4 == t) {
+        n[q]++;
+        s[q] += 6 + (crosses(g, u) ? 1 : 0);
+      }
+  }
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    exit_phase[c * 7 + q] = (uint8_t)(s[q] - p1);
+    count[c * 7 + q] = n[q];
+  }
+}
+
+// Composition of the maps of kSuper consecutive chunks.
+__global__ void super_maps_kernel(int64_t nchunks, const uint8_t *exit_phase,
+                                  const uint32_t *count, uint8_t *sexit, uint32_t *scount) {
+  const int64_t sc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c0 = sc * kSuper;
+  if (c0 >= nchunks) return;
+  const int64_t c1 = min(nchunks, c0 + kSuper);
+  for (int q = 0; q < 7; q++) {
+    int ph = q;
+    uint32_t tot = 0;
+    for (int64_t c = c0; c < c1; c++) {
+      tot += count[c * 7 + ph];
+      ph = exit_phase[c * 7 + ph];
+    }
+    sexit[sc * 7 + q] = (uint8_t)ph;
+    scount[sc * 7 + q] = tot;
+  }
+}
+
+// One thread: entry phase and first wire of every super-chunk.
+__global__ void super_scan_kernel(int64_t nsuper, const uint8_t *sexit, const uint32_t *scount,
+                                  uint8_t *sphase, uint64_t *sbase) {
+  int ph = 0;
+  uint64_t tot = 0;
+  for (int64_t sc = 0; sc < nsuper; sc++) {
+    sphase[sc] = (uint8_t)ph;
+    sbase[sc] = tot;
+    tot += scount[sc * 7 + ph];
+    ph = sexit[sc * 7 + ph];
+  }
+}
+
+// Entry phase and first wire of every chunk.
+__global__ void chunk_scan_kernel(int64_t nchunks, const uint8_t *exit_phase,
+                                  const uint32_t *count, const uint8_t *sphase,
+                                  const uint64_t *sbase, uint8_t *cphase, uint64_t *cbase) {
+  const int64_t sc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c0 = sc * kSuper;
+  if (c0 >= nchunks) return;
+  const int64_t c1 = min(nchunks, c0 + kSuper);
+  int ph = sphase[sc];
+  uint64_t tot = sbase[sc];
+  for (int64_t c = c0; c < c1; c++) {
+    cphase[c] = (uint8_t)ph;
+    cbase[c] = tot;
+    tot += count[c * 7 + ph];
+    ph = exit_phase[c * 7 + ph];
+  }
+}
+
+// Every chunk emits its wires (circuit.cc:1158-1186).
+__global__ void gen_wires_kernel(GenArgs g, int64_t base, int64_t nchunks, const uint8_t *cphase,
+                                 const uint64_t *cbase, uint32_t *in_ptr, uint32_t *out_ptr,
+                                 float *L, float *R, float *C, int32_t *locator) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchunks) return;
+  int64_t w = (int64_t)cbase[c];
+  if (w >= g.W) return;
+  const int64_t p0 = base + c * kChunk, p1 = p0 + kChunk;
+  int64_t s = p0 + cphase[c];
+  uint64_t x = skip(g.seed_state, (uint64_t)s);
+  while (s < p1 && w < g.W) {
+    const double uR = draw(x), uL = draw(x), uC = draw(x), uIn = draw(x), uPct = draw(x);
+    const uint32_t n = (uint32_t)(w / g.wpp);
+    R[w] = __double2float_rn(__dadd_rn(__dmul_rn(uR, 10.0), 1.0));
+    L[w] = __double2float_rn(__dadd_rn(__dmul_rn(uL, g.L_scale), g.L_off));
+    C[w] = __double2float_rn(__dmul_rn(uC, 0.1));
+    in_ptr[w] = pick(uIn, n, (uint32_t)g.npp);
+    if (!crosses(g, uPct)) {
+      out_ptr[w] = pick(draw(x), n, (uint32_t)g.npp);
+      s += 6;
+    } else {
+      int nn = (int)(draw(x) * (double)(g.P - 1));
+      if (nn >= (int)n) nn++;
+      const uint32_t o = pick(draw(x), (uint32_t)nn, (uint32_t)g.npp);
+      out_ptr[w] = o;
+      locator[o] = 0;
+      s += 7;
+    }
+    w++;
+  }
+}
+
+// Locations (circuit.cc:1228-1244) and node degrees.
+__global__ void gen_locs_kernel(GenArgs g, const uint32_t *in_ptr, const uint32_t *out_ptr,
+                                const int32_t *locator, uint8_t *in_loc, uint8_t *out_loc,
+                                uint32_t *deg) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= g.W) return;
+  const uint32_t n = (uint32_t)(w / g.wpp), a = in_ptr[w], b = out_ptr[w];
+  in_loc[w] = locator[a] ? CKT_PRIVATE_PTR : CKT_SHARED_PTR;
+  out_loc[w] = (b / (uint32_t)g.npp != n) ? CKT_GHOST_PTR
+                                          : (locator[b] ? CKT_PRIVATE_PTR : CKT_SHARED_PTR);
+  atomicAdd(deg + a, 1u);
+  atomicAdd(deg + b, 1u);
+}
+
+// Exclusive scan of deg[0..n) into off[0..n] (off[n] = total), three passes.
+constexpr int kScanBlock = 1024, kScanItems = 4;
+
+__global__ void scan_blocks_kernel(const uint32_t *in, int64_t n, uint32_t *out, uint32_t *sums) {
+  __shared__ uint32_t warp_tot[32];
+  const int64_t i0 = ((int64_t)blockIdx.x * kScanBlock + threadIdx.x) * kScanItems;
+  uint32_t v[kScanItems], t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
+    t += v[k];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t incl = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = warp_tot[lane], wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    warp_tot[lane] = wi - w;  // exclusive prefix of warp totals
+    if (lane == 31) sums[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  uint32_t run = warp_tot[wid] + incl - t;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (i0 + k < n) out[i0 + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void scan_sums_kernel(uint32_t *sums, int64_t nblocks, uint32_t *total) {
+  uint32_t run = 0;
+  for (int64_t b = 0; b < nblocks; b++) {
+    const uint32_t v = sums[b];
+    sums[b] = run;
+    run += v;
+  }
+  *total = run;
+}
+
+__global__ void scan_add_kernel(uint32_t *out, int64_t n, const uint32_t *sums) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / ((int64_t)kScanBlock * kScanItems)];
+}
+
+__global__ void csr_fill_kernel(int64_t W, const uint32_t *in_ptr, const uint32_t *out_ptr,
+                                uint32_t *cursor, uint32_t *tmp) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= W) return;
+  tmp[atomicAdd(cursor + in_ptr[w], 1u)] = (uint32_t)(w << 1);
+  tmp[atomicAdd(cursor + out_ptr[w], 1u)] = (uint32_t)(w << 1) | 1u;
+}
+
+// Per node: sort its contributions by (wire, end), then write the entries
+// with their piece-group flags, the wire ends' slots and the flag bits, and
+// mark private nodes in the offsets.
+__global__ void csr_finish_kernel(GenArgs g, uint32_t *off, const int32_t *locator, uint32_t *tmp,
+                                  uint32_t *ent, uint32_t *slot_in, uint32_t *slot_out,
+                                  uint32_t *gstart) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= g.N) return;
+  const uint32_t b = off[x] & 0x7fffffffu, e = off[x + 1] & 0x7fffffffu;
+  for (uint32_t i = b + 1; i < e; i++) {
+    const uint32_t v = tmp[i];
+    uint32_t j = i;
+    while (j > b && tmp[j - 1] > v) {
+      tmp[j] = tmp[j - 1];
+      j--;
+    }
+    tmp[j] = v;
+  }
+  int64_t last_piece = -1;
+  for (uint32_t i = b; i < e; i++) {
+    const uint32_t v = tmp[i], w = v >> 1, end = v & 1u;
+    const int64_t piece = w / g.wpp;
+    const uint32_t start = piece != last_piece ? 1u : 0u;
+    last_piece = piece;
+    ent[i] = (w << 2) | (end << 1) | start;
+    if (end) slot_out[w] = i;
+    else slot_in[w] = i;
+    if (start) atomicOr(gstart + (i >> 5), 1u << (i & 31));
+  }
+  if (locator[x]) atomicOr(off + x, kPrivateBit);
+}
+
+}  // namespace
+}  // namespace ckt
+
+using namespace ckt;
+
+extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *o, void *stream) {
+  CKT_REQUIRE(p != nullptr && o != nullptr, "NULL argument");
+  const int32_t P = p->num_pieces, npp = p->nodes_per_piece, wpp = p->wires_per_piece;
+  CKT_REQUIRE(P >= 1 && npp >= 1 && wpp >= 0, "bad shape P=%d npp=%d wpp=%d", P, npp, wpp);
+  const int64_t N = (int64_t)P * npp, W = (int64_t)P * wpp;
+  CKT_REQUIRE(N < 0x7fffffffLL && W <= kMaxWires, "circuit too large (N=%lld W=%lld)",
+              (long long)N, (long long)W);
+  CKT_REQUIRE(o->charge && o->node_voltage && o->node_capacitance && o->node_leakage &&
+                  o->locator && o->off,
+              "node arrays are NULL");
+  CKT_REQUIRE(W == 0 || (o->in_ptr && o->out_ptr && o->in_loc && o->out_loc && o->inductance &&
+                         o->resistance && o->capacitance && o->current && o->voltage && o->ent &&
+                         o->slot_in && o->slot_out && o->gstart),
+              "wire arrays are NULL");
+  const cudaStream_t s = as_stream(stream);
+  static const Jump jump = make_jump();
+  CKT_CUDA(cudaMemcpyToSymbolAsync(g_jump, &jump, sizeof(Jump), 0, cudaMemcpyHostToDevice, s));
+  GenArgs g;
+  g.P = P; g.npp = npp; g.wpp = wpp;
+  g.pct = p->pct_wire_in_piece; g.L_off = p->L_offset; g.L_scale = p->L_scale;
+  g.seed_state = (((uint64_t)p->random_seed & 0xffffffffull) << 16) | 0x330Eull;
+  g.W = W; g.N = N;
+
+  gen_nodes_kernel<<<grid_for((N + 15) / 16), 256, 0, s>>>(g, o->charge, o->node_voltage,
+                                                          o->node_capacitance, o->node_leakage,
+                                                          o->locator);
+  CKT_CHECK_LAUNCH();
+  CKT_CUDA(cudaMemsetAsync(o->off, 0, (N + 1) * 4, s));
+  if (W == 0) return CKT_OK;
+
+  // Scratch: chunk maps, scans, degree cursors, unsorted contributions.
+  const int64_t base = 3 * N;
+  const int64_t nchunks = (7 * W + 8 + kChunk - 1) / kChunk;
+  const int64_t nsuper = (nchunks + kSuper - 1) / kSuper;
+  const int64_t scan_blocks = (N + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
+  const size_t sz_exit = nchunks * 7, sz_cnt = nchunks * 7 * 4, sz_sexit = nsuper * 7,
+               sz_scnt = nsuper * 7 * 4, sz_sph = nsuper, sz_sb = nsuper * 8, sz_cph = nchunks,
+               sz_cb = nchunks * 8, sz_deg = (N + 1) * 4, sz_sums = (scan_blocks + 1) * 4,
+               sz_tmp = 2 * W * 4;
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t total = al(sz_exit) + al(sz_cnt) + al(sz_sexit) + al(sz_scnt) + al(sz_sph) +
+                       al(sz_sb) + al(sz_cph) + al(sz_cb) + al(sz_deg) + al(sz_sums) + al(sz_tmp);
+  char *scratch = nullptr;
+  CKT_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), total, s));
+  char *q = scratch;
+  auto take = [&q, &al](size_t b) {
+    char *r = q;
+    q += al(b);
+    return r;
+  };
+  uint8_t *exit_phase = (uint8_t *)take(sz_exit);
+  uint32_t *count = (uint32_t *)take(sz_cnt);
+  uint8_t *sexit = (uint8_t *)take(sz_sexit);
+  uint32_t *scount = (uint32_t *)take(sz_scnt);
+  uint8_t *sphase = (uint8_t *)take(sz_sph);
+  uint64_t *sbase = (uint64_t *)take(sz_sb);
+  uint8_t *cphase = (uint8_t *)take(sz_cph);
+  uint64_t *cbase = (uint64_t *)take(sz_cb);
+  uint32_t *deg = (uint32_t *)take(sz_deg);
+  uint32_t *sums = (uint32_t *)take(sz_sums);
+  uint32_t *tmp = (uint32_t *)take(sz_tmp);
+  int rc = CKT_OK;
+  auto ok = [&rc](cudaError_t e) {
+    if (rc == CKT_OK && e != cudaSuccess)
+      rc = set_error(CKT_ECUDA, "device generator: %s", cudaGetErrorString(e));
+  };
+
+  chunk_maps_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(g, base, nchunks, exit_phase, count);
+  ok(cudaGetLastError());
+  super_maps_kernel<<<grid_for(nsuper, 128), 128, 0, s>>>(nchunks, exit_phase, count, sexit,
+                                                          scount);
+  ok(cudaGetLastError());
+  super_scan_kernel<<<1, 1, 0, s>>>(nsuper, sexit, scount, sphase, sbase);
+  ok(cudaGetLastError());
+  chunk_scan_kernel<<<grid_for(nsuper, 128), 128, 0, s>>>(nchunks, exit_phase, count, sphase,
+                                                          sbase, cphase, cbase);
+  ok(cudaGetLastError());
+  gen_wires_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(
+      g, base, nchunks, cphase, cbase, o->in_ptr, o->out_ptr, o->inductance, o->resistance,
+      o->capacitance, o->locator);
+  ok(cudaGetLastError());
+  ok(cudaMemsetAsync(deg, 0, sz_deg, s));
+  gen_locs_kernel<<<grid_for(W), 256, 0, s>>>(g, o->in_ptr, o->out_ptr, o->locator, o->in_loc,
+                                              o->out_loc, deg);
+  ok(cudaGetLastError());
+  scan_blocks_kernel<<<(unsigned)scan_blocks, kScanBlock, 0, s>>>(deg, N, o->off, sums);
+  ok(cudaGetLastError());
+  scan_sums_kernel<<<1, 1, 0, s>>>(sums, scan_blocks, o->off + N);
+  ok(cudaGetLastError());
+  scan_add_kernel<<<grid_for(N), 256, 0, s>>>(o->off, N, sums);
+  ok(cudaGetLastError());
+  ok(cudaMemcpyAsync(deg, o->off, N * 4, cudaMemcpyDeviceToDevice, s));  // fill cursors
+  csr_fill_kernel<<<grid_for(W), 256, 0, s>>>(W, o->in_ptr, o->out_ptr, deg, tmp);
+  ok(cudaGetLastError());
+  ok(cudaMemsetAsync(o->gstart, 0, ((2 * W + 31) / 32) * 4, s));
+  csr_finish_kernel<<<grid_for(N), 256, 0, s>>>(g, o->off, o->locator, tmp, o->ent, o->slot_in,
+                                                o->slot_out, o->gstart);
+  ok(cudaGetLastError());
+  ok(cudaMemsetAsync(o->current, 0, 10 * W * 4, s));
+  ok(cudaMemsetAsync(o->voltage, 0, 9 * W * 4, s));
+  cudaFreeAsync(scratch, s);
+  return rc;
+}

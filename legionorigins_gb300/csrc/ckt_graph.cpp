@@ -221,6 +221,21 @@ int ckt_graph_destroy(ckt_graph *graph) {
   return CKT_OK;
 }
 
+int ckt_graph_export(const ckt_graph *g, uint32_t *off, uint32_t *ent, uint32_t *slot_in,
+                     uint32_t *slot_out, uint32_t *gstart) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  const int64_t W = g->W, N = g->N;
+  if (off) CKT_CUDA(cudaMemcpy(off, g->node_off, (N + 1) * 4, cudaMemcpyDeviceToHost));
+  if (W > 0) {
+    if (ent) CKT_CUDA(cudaMemcpy(ent, g->node_ent, 2 * W * 4, cudaMemcpyDeviceToHost));
+    if (slot_in) CKT_CUDA(cudaMemcpy(slot_in, g->slot_in, W * 4, cudaMemcpyDeviceToHost));
+    if (slot_out) CKT_CUDA(cudaMemcpy(slot_out, g->slot_out, W * 4, cudaMemcpyDeviceToHost));
+    if (gstart)
+      CKT_CUDA(cudaMemcpy(gstart, g->gstart, ((2 * W + 31) / 32) * 4, cudaMemcpyDeviceToHost));
+  }
+  return CKT_OK;
+}
+
 int ckt_graph_info(const ckt_graph *g, int64_t *num_wires, int64_t *num_nodes,
                    int32_t *num_pieces, int64_t *device_bytes) {
   CKT_REQUIRE(g != nullptr, "graph is NULL");

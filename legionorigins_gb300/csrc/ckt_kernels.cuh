@@ -25,6 +25,14 @@ namespace ckt {
 template <int MODE>
 struct WireStep;
 
+// Correctly rounded a / b.  A NaN dividend gives the quiet NaN every GPU
+// arithmetic instruction returns for NaN operands (0x7fffffff, the same bits
+// __fdiv_rn produces) without entering the divide routine's special-case
+// path; once the recurrence has overflowed, every dividend is NaN.
+__device__ __forceinline__ float div_rn(float a, float b) {
+  return (a != a) ? __int_as_float(0x7fffffff) : __fdiv_rn(a, b);
+}
+
 // EXACT: ((dv) - (L*(i-I0))/dt) / R and V0 + (dt*(i_k - i_k+1))/C, each
 // operation rounded exactly as the reference's fp32 source.
 template <>
@@ -36,12 +44,12 @@ struct WireStep<CKT_MODE_EXACT> {
 #pragma unroll
     for (int k = 0; k < 10; k++) {
       const float dv = __fsub_rn(nv[k + 1], nv[k]);
-      const float q = __fdiv_rn(__fmul_rn(L, __fsub_rn(ni[k], I0[k])), dt);
-      ni[k] = __fdiv_rn(__fsub_rn(dv, q), R);
+      const float q = div_rn(__fmul_rn(L, __fsub_rn(ni[k], I0[k])), dt);
+      ni[k] = div_rn(__fsub_rn(dv, q), R);
     }
 #pragma unroll
     for (int k = 0; k < 9; k++)
-      nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(__fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1])), C));
+      nv[k + 1] = __fadd_rn(V0[k], div_rn(__fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1])), C));
   }
 };
 
@@ -276,13 +284,31 @@ __device__ __forceinline__ void dc_block(uint32_t x0, uint32_t xe,
   }
   for (uint32_t c0 = lo; c0 < hi; c0 += kDcChunk) {
     const uint32_t cn = min(kDcChunk, hi - c0);
-#pragma unroll 4
-    for (uint32_t j = threadIdx.x; j < cn; j += BLOCK) {
-      const uint32_t u = ent[c0 + j];
-      const uint32_t w = u >> 2;
-      sval[j] = (u & 2u) ? __fmul_rn(dt, ld_f32<COHERENT>(I9 + w))
-                         : __fmul_rn(-dt, ld_f32<COHERENT>(I0 + w));
-      sflag[j] = (uint8_t)(u & 1u);
+    // Stage in batches of kDcBatch entries per thread: all entry loads of a
+    // batch first, then all of its current gathers, so every thread keeps
+    // kDcBatch independent loads in flight at each of the two levels.
+    constexpr uint32_t kDcBatch = 8;
+    for (uint32_t j0 = 0; j0 < cn; j0 += kDcBatch * BLOCK) {
+      uint32_t u[kDcBatch];
+#pragma unroll
+      for (uint32_t r = 0; r < kDcBatch; r++) {
+        const uint32_t j = j0 + r * BLOCK + threadIdx.x;
+        u[r] = j < cn ? ent[c0 + j] : 0u;
+      }
+      float v[kDcBatch];
+#pragma unroll
+      for (uint32_t r = 0; r < kDcBatch; r++) {
+        const uint32_t w = u[r] >> 2;
+        v[r] = (u[r] & 2u) ? ld_f32<COHERENT>(I9 + w) : ld_f32<COHERENT>(I0 + w);
+      }
+#pragma unroll
+      for (uint32_t r = 0; r < kDcBatch; r++) {
+        const uint32_t j = j0 + r * BLOCK + threadIdx.x;
+        if (j < cn) {
+          sval[j] = (u[r] & 2u) ? __fmul_rn(dt, v[r]) : __fmul_rn(-dt, v[r]);
+          sflag[j] = (uint8_t)(u[r] & 1u);
+        }
+      }
     }
     __syncthreads();
     const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
