@@ -170,6 +170,20 @@ int ckt_apply_fold(const ckt_graph *graph, int32_t piece_index, float *shr_fold,
 int ckt_update_voltages(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
                         const int32_t *locator, void *stream);
 
+/* Blocking forms of the three tasks, with the reference's synchronous
+ * semantics: its GPU task bodies return only after cudaDeviceSynchronize
+ * (apps/circuit/circuit_gpu.cu:204, 303, 367).  Each launches exactly like
+ * its asynchronous form, then waits for `stream` and returns CKT_ECUDA when
+ * the launch or the work on the device failed. */
+int ckt_calc_new_currents_sync(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                               ckt_nodes shr, ckt_nodes ghost, const ckt_params *prm,
+                               void *stream);
+int ckt_distribute_charge_sync(const ckt_graph *graph, int32_t piece_index, ckt_wires wires,
+                               ckt_nodes pvt, float *shr_fold, float *ghost_fold,
+                               const ckt_params *prm, void *stream);
+int ckt_update_voltages_sync(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
+                             const int32_t *locator, void *stream);
+
 /* Replaces sanity_check_wires_gpu (apps/circuit/circuit.h:103-104,
  * apps/circuit/circuit_gpu.cu:151-217) without its asserts: validates every
  * wire of the piece (locations in range, in-node inside the piece,
@@ -460,6 +474,63 @@ int ckt_server_destroy(ckt_server *server);
  * write.
  * ---------------------------------------------------------------------- */
 int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, int32_t paired, float *sink, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Reduction microbenchmark: the GPU form of benchmarks/reductions/
+ * reducetest.cc.  A histogram of `buckets` unsigned counters receives one
+ * +1 reduction per element; element i of batch b has key
+ * myrand(start + i) % buckets with start = b * batch_size (32-bit unsigned
+ * arithmetic, reducetest.cc:174, 323-347).  The schedules are the
+ * benchmark's cases mapped onto the GPU's memory levels; every schedule adds
+ * the same counts (integer addition: the order does not matter).
+ * ---------------------------------------------------------------------- */
+typedef enum {
+  /* original / redsingle (reducetest.cc:335-348, 428-452): every element
+   * reduces straight into the target instance -- one global atomic add. */
+  CKT_RED_SINGLE = 0,
+  /* redfold (:378-400): a fold instance per thread block, initialised to the
+   * identity, receives the block's reductions and is then applied to the
+   * target.  The fold lives in shared memory when buckets <=
+   * CKT_HIST_SMEM_FOLD_BUCKETS, otherwise in a few L2-resident copies in the
+   * scratch buffer. */
+  CKT_RED_FOLD = 1,
+  /* localize (:351-375): the owner of a range of buckets copies that range
+   * of the target into its shared memory, applies every reduction that falls
+   * in it without global atomics, and copies it back; the reductions are
+   * first routed to their owners (keyed, counted, scattered by range). */
+  CKT_RED_LOCALIZE = 2,
+  /* redlist (:403-425): each batch appends (pointer, value) entries to a
+   * reduction list in the scratch buffer; the lists are then applied to the
+   * target. */
+  CKT_RED_LIST = 3
+} ckt_red_schedule;
+
+#define CKT_HIST_SMEM_FOLD_BUCKETS 51200     /* 200 KB of 32-bit counters */
+#define CKT_HIST_LOCALIZE_MAX_BUCKETS 67108864 /* 4096 ranges x 16384 buckets */
+
+typedef struct {
+  uint32_t buckets;     /* -buckets (default 1048576); >= 1 */
+  uint32_t batch_size;  /* -bsize (default 1048576) */
+  uint32_t num_batches; /* -batches (default 1024) */
+  uint32_t first_batch; /* index of the first batch (0 in the benchmark) */
+  uint32_t seed1;       /* 12345 (reducetest.cc:208) */
+  uint32_t seed2;       /* 54321 (reducetest.cc:209) */
+} ckt_hist_params;
+
+/* The benchmark's defaults (reducetest.cc:205-209). */
+void ckt_hist_default_params(ckt_hist_params *out);
+/* Scratch bytes a schedule needs: *min_bytes at least (0 when it needs
+ * none), *good_bytes for full speed (L2-sized rounds). */
+int ckt_hist_scratch_bytes(const ckt_hist_params *p, int32_t schedule, uint64_t *min_bytes,
+                           uint64_t *good_bytes);
+/* Adds every batch's counts into hist[0..buckets) (device memory; its
+ * contents are kept, like the benchmark's master instance).  `scratch` is
+ * device memory of `scratch_bytes` >= the schedule's minimum, 16-byte
+ * aligned, owned by the caller, free for the call's duration; its contents
+ * need no initialisation and are left undefined.  Asynchronous on
+ * `stream`. */
+int ckt_hist_run(const ckt_hist_params *p, int32_t schedule, uint32_t *hist, void *scratch,
+                 uint64_t scratch_bytes, void *stream);
 
 #ifdef __cplusplus
 }

@@ -106,6 +106,14 @@ class DeviceCircuitArrays(ctypes.Structure):
         "locator", "off", "ent", "slot_in", "slot_out", "gstart")]
 
 
+class HistParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "buckets", "batch_size", "num_batches", "first_batch", "seed1", "seed2")]
+
+
+RED_SINGLE, RED_FOLD, RED_LOCALIZE, RED_LIST = 0, 1, 2, 3
+
+
 # (name, restype, argtypes) of every exported symbol declared in include/ckt.h
 _P = ctypes.c_void_p
 _I32, _I64, _U32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32
@@ -120,6 +128,11 @@ SIGNATURES = {
                                              ctypes.POINTER(Params), _P]),
     "ckt_apply_fold": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P]),
     "ckt_update_voltages": (ctypes.c_int, [ctypes.POINTER(Piece), Nodes, Nodes, _P, _P]),
+    "ckt_calc_new_currents_sync": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, Nodes, Nodes,
+                                                  Nodes, ctypes.POINTER(Params), _P]),
+    "ckt_distribute_charge_sync": (ctypes.c_int, [_P, _I32, Wires, Nodes, _P, _P,
+                                                  ctypes.POINTER(Params), _P]),
+    "ckt_update_voltages_sync": (ctypes.c_int, [ctypes.POINTER(Piece), Nodes, Nodes, _P, _P]),
     "ckt_sanity_check_wires": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, _U32,
                                               ctypes.POINTER(_I64), _P]),
     "ckt_calc_new_currents_all": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _P]),
@@ -132,6 +145,12 @@ SIGNATURES = {
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
     "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
+    "ckt_hist_default_params": (None, [ctypes.POINTER(HistParams)]),
+    "ckt_hist_scratch_bytes": (ctypes.c_int, [ctypes.POINTER(HistParams), _I32,
+                                              ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_uint64)]),
+    "ckt_hist_run": (ctypes.c_int, [ctypes.POINTER(HistParams), _I32, _P, _P, ctypes.c_uint64,
+                                    _P]),
     "ckt_sanity_check_pieces_noalloc": (ctypes.c_int, [ctypes.POINTER(Piece), _I32, Wires, _U32,
                                                        ctypes.POINTER(_I64), _P]),
     "ckt_batch_create": (ctypes.c_int, [_I32, ctypes.POINTER(GenParams),

@@ -150,24 +150,28 @@ class DeviceCircuit:
         check(L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), stream))
         check(L.ckt_update_voltages_all(g, n, stream))
 
-    def loop_per_piece(self, prm: Params, stream: int = 0) -> None:
+    def loop_per_piece(self, prm: Params, stream: int = 0, blocking: bool = False) -> None:
         """One outer loop as the reference's per-piece task calls: CNC for
         every piece; DC for every piece, each followed by the application of
         that piece's reduction instances (the runtime applies a point's
         instances once the point finishes, points in ascending order; the
         two fold buffers are reused, and ckt_apply_fold returns them to the
-        identity); UV for every piece."""
+        identity); UV for every piece.  `blocking` uses the *_sync forms,
+        which wait for the device after every task like the reference's GPU
+        task bodies."""
         L, g, w, n = lib(), self.graph.handle, self.wires(), self.nodes()
+        cnc = L.ckt_calc_new_currents_sync if blocking else L.ckt_calc_new_currents
+        dc = L.ckt_distribute_charge_sync if blocking else L.ckt_distribute_charge
+        uv = L.ckt_update_voltages_sync if blocking else L.ckt_update_voltages
         locator = self.t["locator"].data_ptr()
         for k in range(len(self.pieces)):
-            check(L.ckt_calc_new_currents(ctypes.byref(self.pieces[k]), w, n, n, n,
-                                          ctypes.byref(prm), stream))
+            check(cnc(ctypes.byref(self.pieces[k]), w, n, n, n, ctypes.byref(prm), stream))
         sf, gf = self.shr_fold.data_ptr(), self.ghost_fold.data_ptr()
         for k in range(len(self.pieces)):
-            check(L.ckt_distribute_charge(g, k, w, n, sf, gf, ctypes.byref(prm), stream))
+            check(dc(g, k, w, n, sf, gf, ctypes.byref(prm), stream))
             check(L.ckt_apply_fold(g, k, sf, gf, n.charge, stream))
         for k in range(len(self.pieces)):
-            check(L.ckt_update_voltages(ctypes.byref(self.pieces[k]), n, n, locator, stream))
+            check(uv(ctypes.byref(self.pieces[k]), n, n, locator, stream))
 
     def sanity_check(self, stream: int = 0) -> None:
         bad = ctypes.c_int64()

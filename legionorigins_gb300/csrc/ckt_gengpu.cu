@@ -345,7 +345,14 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
                                                           o->locator);
   CKT_CHECK_LAUNCH();
   CKT_CUDA(cudaMemsetAsync(o->off, 0, (N + 1) * 4, s));
-  if (W == 0) return CKT_OK;
+  if (W == 0) {
+    // No contributions: only the private-node flags of the offsets remain
+    // (every node is private); the entry arrays are never touched.
+    csr_finish_kernel<<<grid_for(N), 256, 0, s>>>(g, o->off, o->locator, nullptr, nullptr,
+                                                  nullptr, nullptr, nullptr);
+    CKT_CHECK_LAUNCH();
+    return CKT_OK;
+  }
 
   // Scratch: chunk maps, scans, degree cursors, unsorted contributions.
   const int64_t base = 3 * N;

@@ -94,6 +94,14 @@ static int check_graph_wires(const ckt_graph *g, const ckt_wires &w) {
   return CKT_OK;
 }
 
+// Completion wait of the blocking task forms.
+static int wait_stream(void *stream, const char *task) {
+  const cudaError_t e = cudaStreamSynchronize(as_stream(stream));
+  if (e != cudaSuccess)
+    return set_error(CKT_ECUDA, "%s failed on the device: %s", task, cudaGetErrorString(e));
+  return CKT_OK;
+}
+
 }  // namespace ckt
 
 using namespace ckt;
@@ -160,8 +168,6 @@ int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires
               piece_index, graph->P);
   if (graph->pieces[piece_index].num_wires == 0) return CKT_OK;
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
-  CKT_REQUIRE(piece_index >= 0 && piece_index < graph->P, "piece_index %d out of range [0, %d)",
-              piece_index, graph->P);
   CKT_REQUIRE(pvt.charge != nullptr, "pvt.charge is NULL");
   const int64_t t0 = graph->touch_first[piece_index], t1 = graph->touch_first[piece_index + 1];
   if (t1 == t0) return CKT_OK;
@@ -250,6 +256,27 @@ int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *strea
     CKT_CHECK_LAUNCH();
   }
   return CKT_OK;
+}
+
+int ckt_calc_new_currents_sync(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                               ckt_nodes shr, ckt_nodes ghost, const ckt_params *prm,
+                               void *stream) {
+  const int rc = ckt_calc_new_currents(piece, wires, pvt, shr, ghost, prm, stream);
+  return rc ? rc : wait_stream(stream, "calc_new_currents");
+}
+
+int ckt_distribute_charge_sync(const ckt_graph *graph, int32_t piece_index, ckt_wires wires,
+                               ckt_nodes pvt, float *shr_fold, float *ghost_fold,
+                               const ckt_params *prm, void *stream) {
+  const int rc =
+      ckt_distribute_charge(graph, piece_index, wires, pvt, shr_fold, ghost_fold, prm, stream);
+  return rc ? rc : wait_stream(stream, "distribute_charge");
+}
+
+int ckt_update_voltages_sync(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
+                             const int32_t *locator, void *stream) {
+  const int rc = ckt_update_voltages(piece, pvt, shr, locator, stream);
+  return rc ? rc : wait_stream(stream, "update_voltages");
 }
 
 int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num_nodes_total,

@@ -588,3 +588,106 @@ double ocl_baseline_run(const ocl_params *p, int32_t loops, int32_t steps,
   free(s.app_cfirst); free(s.app_slot);
   return elapsed;
 }
+
+/* ------------------------------------------------------------------------
+ * Reduction microbenchmark (benchmarks/reductions/reducetest.cc)
+ * ---------------------------------------------------------------------- */
+
+uint32_t ocl_hist_rand(uint64_t ival, uint32_t seed1, uint32_t seed2)
+{
+  /* reducetest.cc:323-333 */
+  uint64_t r = ival;
+  for (int j = 0; j < 16; j++) {
+    r = (0x5DEECE66DULL * r + 0xBULL) & 0xFFFFFFFFFFFFULL;
+    r ^= ((ival >> j) & 1u) ? seed1 : seed2;
+  }
+  return (uint32_t)r;
+}
+
+static void hist_batches(uint32_t buckets, uint32_t batch_size, uint64_t b0, uint64_t b1,
+                         uint32_t step, uint32_t seed1, uint32_t seed2, uint32_t *hist)
+{
+  /* reducetest.cc:174 (start = i * count, 32-bit unsigned) and :341-347 (the
+   * task loop) */
+  for (uint64_t b = b0; b < b1; b += step) {
+    const uint32_t start = (uint32_t)(b * batch_size);
+    for (uint32_t i = 0; i < batch_size; i++)
+      hist[ocl_hist_rand((uint32_t)(start + i), seed1, seed2) % buckets] += 1u;
+  }
+}
+
+void ocl_histogram(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
+                   uint32_t first_batch, uint32_t seed1, uint32_t seed2, uint32_t *hist)
+{
+  hist_batches(buckets, batch_size, first_batch, (uint64_t)first_batch + num_batches, 1, seed1,
+               seed2, hist);
+}
+
+typedef struct {
+  uint32_t buckets, batch_size, step, seed1, seed2;
+  uint64_t b0, b1;
+  uint32_t *hist;
+  pthread_mutex_t *mu;
+  int failed;
+} hist_job;
+
+static void *hist_worker(void *argp)
+{
+  hist_job *j = (hist_job *)argp;
+  uint32_t *fold = (uint32_t *)calloc(j->buckets, sizeof(uint32_t)); /* identity 0 */
+  if (!fold) {
+    j->failed = 1;
+    return NULL;
+  }
+  hist_batches(j->buckets, j->batch_size, j->b0, j->b1, j->step, j->seed1, j->seed2, fold);
+  pthread_mutex_lock(j->mu);
+  for (uint32_t k = 0; k < j->buckets; k++) j->hist[k] += fold[k];
+  pthread_mutex_unlock(j->mu);
+  free(fold);
+  return NULL;
+}
+
+double ocl_histogram_threads(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
+                             uint32_t first_batch, uint32_t seed1, uint32_t seed2,
+                             int32_t threads, uint32_t *hist)
+{
+  if (buckets == 0 || threads < 1 || !hist) return -1.0;
+  if ((uint32_t)threads > num_batches && num_batches > 0) threads = (int32_t)num_batches;
+  pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
+  hist_job *jobs = (hist_job *)calloc((size_t)threads, sizeof(hist_job));
+  pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  if (!jobs || !tid) {
+    free(jobs);
+    free(tid);
+    return -1.0;
+  }
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  int started = 0, failed = 0;
+  for (int32_t t = 0; t < threads; t++) {
+    hist_job *j = &jobs[t];
+    j->buckets = buckets;
+    j->batch_size = batch_size;
+    j->b0 = (uint64_t)first_batch + (uint32_t)t;
+    j->b1 = (uint64_t)first_batch + num_batches;
+    j->step = (uint32_t)threads;
+    j->seed1 = seed1;
+    j->seed2 = seed2;
+    j->hist = hist;
+    j->mu = &mu;
+    if (pthread_create(&tid[t], NULL, hist_worker, j) != 0) {
+      failed = 1;
+      break;
+    }
+    started++;
+  }
+  for (int t = 0; t < started; t++) {
+    pthread_join(tid[t], NULL);
+    failed |= jobs[t].failed;
+  }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  free(jobs);
+  free(tid);
+  if (failed) return -1.0;
+  return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}

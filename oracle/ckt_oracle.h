@@ -129,6 +129,30 @@ double ocl_baseline_run(const ocl_params *p, int32_t loops, int32_t steps,
                         float *node_charge, float *node_voltage,
                         const float *node_cap, const float *node_leak);
 
+/* ---- Reduction microbenchmark (benchmarks/reductions/reducetest.cc) ---- */
+
+/* myrand (reducetest.cc:323-333): 16 rounds of the 48-bit LCG
+ * r <- (0x5DEECE66D r + 0xB) mod 2^48, each followed by r ^= seed1 when bit
+ * j of ival is set, else seed2; the low 32 bits of r. */
+uint32_t ocl_hist_rand(uint64_t ival, uint32_t seed1, uint32_t seed2);
+
+/* The histogram every reducetest case adds into its master instance: for
+ * batches b = first_batch .. first_batch+num_batches-1 and i < batch_size,
+ * hist[myrand(start + i) % buckets] += 1, with start = b * batch_size and
+ * start + i both 32-bit unsigned as in the benchmark (reducetest.cc:174,
+ * 341-347).  Adds into hist (it is not cleared). */
+void ocl_histogram(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
+                   uint32_t first_batch, uint32_t seed1, uint32_t seed2, uint32_t *hist);
+
+/* The same histogram on `threads` pthreads in the benchmark's fastest CPU
+ * schedule (redfold, reducetest.cc:378-400): batch b runs on thread
+ * b % threads, which reduces into its own fold instance (identity 0) and
+ * applies it to hist under a mutex when it is done.  Returns the elapsed
+ * seconds, or a negative value on error. */
+double ocl_histogram_threads(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
+                             uint32_t first_batch, uint32_t seed1, uint32_t seed2,
+                             int32_t threads, uint32_t *hist);
+
 #ifdef __cplusplus
 }
 #endif

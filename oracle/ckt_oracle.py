@@ -6,9 +6,11 @@ bench.py's CPU-baseline leg, never by the product package.
 
 The oracle restates the reference circuit application's generator and leaf
 tasks (LegionOrigins apps/circuit/circuit.cc:352-460, 1071-1307 and
-apps/circuit/circuit_gpu.cu:61-149); ckt_oracle.h lists the file:line each
-function follows.  Its parity is pinned by tests/test_oracle_pin.py against
-the reference's own circuit.cc compiled through oracle/refshim.
+apps/circuit/circuit_gpu.cu:61-149) and the reduction microbenchmark's
+histogram (benchmarks/reductions/reducetest.cc:174, 323-347); ckt_oracle.h
+lists the file:line each function follows.  Its parity is pinned by
+tests/test_oracle_pin.py against the reference's own circuit.cc and
+reducetest.cc, compiled through oracle/refshim and oracle/refshim_lowlevel.
 """
 from __future__ import annotations
 
@@ -22,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libckt_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "circuit_ref")
+REDUCE_REF_BIN = os.path.join(HERE, "_ref", "reducetest_ref")
 SEGMENTS = 10
 PRIVATE, SHARED, GHOST = 0, 1, 2
 
@@ -79,6 +82,13 @@ def lib():
         L.ocl_simulate_f64.argtypes = [ctypes.POINTER(_Params), i32, i32, i32] + [P] * 13
         L.ocl_baseline_run.argtypes = [ctypes.POINTER(_Params), i32, i32, i32, i32, i32] + [P] * 13
         L.ocl_baseline_run.restype = ctypes.c_double
+        u32, u64 = ctypes.c_uint32, ctypes.c_uint64
+        L.ocl_hist_rand.argtypes = [u64, u32, u32]
+        L.ocl_hist_rand.restype = u32
+        L.ocl_histogram.argtypes = [u32] * 6 + [P]
+        L.ocl_histogram.restype = None
+        L.ocl_histogram_threads.argtypes = [u32] * 6 + [i32, P]
+        L.ocl_histogram_threads.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -292,3 +302,42 @@ def run_reference(p: GenParams, loops: int, workdir: str, override: Circuit | No
         loc = np.fromfile(f"{pre}.{stage}.r2.bin", "<i4")
         out.append(circuit_from_aos(p, nodes, wires, loc))
     return out[0], out[1]
+
+
+# -- reduction microbenchmark (benchmarks/reductions/reducetest.cc) ------------
+HIST_SEEDS = (12345, 54321)  # reducetest.cc:208-209
+
+
+def histogram(buckets: int, batch_size: int, num_batches: int, first_batch: int = 0,
+              seed1: int = HIST_SEEDS[0], seed2: int = HIST_SEEDS[1]) -> np.ndarray:
+    """The histogram one reducetest case adds into its master instance."""
+    h = np.zeros(buckets, np.uint32)
+    lib().ocl_histogram(buckets, batch_size, num_batches, first_batch, seed1, seed2, _p(h))
+    return h
+
+
+def histogram_threads(buckets: int, batch_size: int, num_batches: int, threads: int,
+                      first_batch: int = 0, seed1: int = HIST_SEEDS[0],
+                      seed2: int = HIST_SEEDS[1]):
+    """(histogram, seconds) on `threads` CPU threads in the redfold schedule."""
+    h = np.zeros(buckets, np.uint32)
+    secs = lib().ocl_histogram_threads(buckets, batch_size, num_batches, first_batch, seed1,
+                                       seed2, threads, _p(h))
+    if secs < 0:
+        raise RuntimeError("ocl_histogram_threads failed")
+    return h, secs
+
+
+def run_reducetest(buckets: int, num_batches: int, batch_size: int, workdir: str) -> np.ndarray:
+    """Run the reference's reducetest.cc (its default cases redfold, localize
+    and redlist, all adding into one master instance) and return the master
+    histogram it leaves behind."""
+    if not os.path.exists(REDUCE_REF_BIN):
+        raise FileNotFoundError(REDUCE_REF_BIN)
+    os.makedirs(workdir, exist_ok=True)
+    path = os.path.join(workdir, "master.bin")
+    env = dict(os.environ, CKT_REFSHIM_DUMP=path)
+    args = [REDUCE_REF_BIN, "-buckets", str(buckets), "-batches", str(num_batches),
+            "-bsize", str(batch_size)]
+    subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL)
+    return np.fromfile(path, "<u4")

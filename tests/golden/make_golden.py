@@ -17,8 +17,15 @@ Fixtures:
                    and voltages) so every value stays finite and the
                    arithmetic is pinned bit for bit.
 
+  hist_<name>.npz  the master histogram the reference's reduction
+                   microbenchmark (benchmarks/reductions/reducetest.cc,
+                   compiled unmodified through oracle/refshim_lowlevel)
+                   leaves after its default cases redfold, localize and
+                   redlist, each of which adds the full histogram into it.
+
 Run in a tree where the reference is present:
     python tests/golden/make_golden.py [--reference /path/to/LegionOrigins]
+                                       [--only circuit|hist]
 """
 from __future__ import annotations
 
@@ -54,6 +61,17 @@ SIM_CASES = {
     "conv_p6n16w64pct0": ((6, 16, 64, 0, 11), 1, 4),
 }
 
+HIST_CASES = {
+    # name: (buckets, batches, batch size)
+    "b1000_n8_s5000": (1000, 8, 5000),
+    "b1_n2_s100": (1, 2, 100),                     # one bucket takes everything
+    "b65537_n5_s7777": (65537, 5, 7777),           # ragged sizes
+    "b4096_n3_s65536": (4096, 3, 65536),
+    "b1048576_n4_s65536": (1048576, 4, 65536),     # the benchmark's bucket count
+    "b7_n3_s0": (7, 3, 0),                         # empty batches
+}
+HIST_CASES_RUN = 3  # redfold, localize, redlist (reducetest.cc:259-261)
+
 FIELDS = ["in_ptr", "out_ptr", "in_loc", "out_loc", "L", "R", "C", "current", "voltage",
           "charge", "node_voltage", "cap", "leak", "locator"]
 
@@ -79,10 +97,20 @@ def save(path: str, c: O.Circuit, **extra) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["circuit", "hist"], default=None)
     args = ap.parse_args()
     if O.build_ref(args.reference) is None:
         sys.exit(f"reference tree not found at {args.reference}")
     work = tempfile.mkdtemp(prefix="ckt_golden_")
+    if args.only != "circuit":
+        for name, (buckets, batches, bsize) in HIST_CASES.items():
+            master = O.run_reducetest(buckets, batches, bsize, os.path.join(work, name))
+            np.savez_compressed(os.path.join(HERE, f"hist_{name}.npz"), master=master,
+                                params=np.array([buckets, batches, bsize], np.int64),
+                                cases=np.array(HIST_CASES_RUN))
+            print("wrote", f"hist_{name}.npz")
+    if args.only == "hist":
+        return
     for name, (P, npp, wpp, pct, seed) in GEN_CASES.items():
         p = O.GenParams(P, npp, wpp, pct, seed)
         init, _ = O.run_reference(p, 1, os.path.join(work, name))

@@ -37,12 +37,15 @@ def device(cuda, c):
                                                  p.wires_per_piece))
 
 
-def run_gpu(cuda, dc, loops, steps, mode, init=0, per_piece=False):
+def run_gpu(cuda, dc, loops, steps, mode, init=0, per_piece=False, blocking=False):
     from legionorigins_gb300 import circuit as C
 
     prm = C.params(steps, mode, init)
     for _ in range(loops):
-        (dc.loop_per_piece if per_piece else dc.loop_index_space)(prm)
+        if per_piece:
+            dc.loop_per_piece(prm, blocking=blocking)
+        else:
+            dc.loop_index_space(prm)
     cuda.cuda.synchronize()
     return dc.to_host()
 
@@ -124,6 +127,28 @@ def test_per_piece_calls_equal_index_space(cuda, oracle, shape):
     oracle.simulate(c, 3, 4)
     for k in STATE:
         assert same_bits(a[k], getattr(c, k)), k
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_blocking_task_forms_equal_async(cuda, oracle, mode):
+    """ckt_*_sync (a device wait after every task, like the reference's GPU
+    task bodies) gives the same bits as the asynchronous calls."""
+    c = oracle.generate(oracle.GenParams(*SHAPES["heavy_reduction"], L_offset=0.001))
+    a = run_gpu(cuda, device(cuda, c), 2, 3, mode=mode, per_piece=True, blocking=True)
+    b = run_gpu(cuda, device(cuda, c), 2, 3, mode=mode, per_piece=True)
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+
+
+def test_blocking_form_reports_bad_arguments(cuda):
+    import ctypes
+
+    from legionorigins_gb300 import CktError, Nodes, Piece, check, lib
+
+    piece = Piece(0, 4, 0, 4)
+    rc = lib().ckt_update_voltages_sync(ctypes.byref(piece), Nodes(), Nodes(), None, None)
+    with pytest.raises(CktError):
+        check(rc)
 
 
 @pytest.mark.parametrize("steps,loops", [(1, 1), (2, 1), (3, 2), (4, 2), (6, 1)])

@@ -122,3 +122,37 @@ def test_entry_points_validate_arguments(ckt):
     assert L.ckt_distribute_charge_all(None, w, n, ctypes.byref(prm), None) == 1
     assert L.ckt_update_voltages_all(None, n, None) == 1
     assert L.ckt_apply_fold(None, 0, None, None, None, None) == 1
+
+
+def test_hist_entry_points_validate_arguments(ckt):
+    """The reduction microbenchmark's checks run before any CUDA call."""
+    from legionorigins_gb300 import reductions as R
+
+    L = ckt.lib()
+    d = ckt.HistParams()
+    L.ckt_hist_default_params(ctypes.byref(d))
+    assert (d.buckets, d.batch_size, d.num_batches, d.seed1, d.seed2) == (
+        1048576, 1048576, 1024, 12345, 54321)
+    assert (d.buckets, d.batch_size, d.num_batches) == tuple(
+        getattr(R.params(), k) for k in ("buckets", "batch_size", "num_batches"))
+    bad = R.params(buckets=0)
+    assert L.ckt_hist_run(ctypes.byref(bad), 0, 8, None, 0, None) == 1
+    assert b"buckets" in L.ckt_last_error()
+    p = R.params(buckets=16, batch_size=4, num_batches=2)
+    assert L.ckt_hist_run(ctypes.byref(p), 9, 8, None, 0, None) == 1
+    assert b"schedule" in L.ckt_last_error()
+    assert L.ckt_hist_run(ctypes.byref(p), 0, None, None, 0, None) == 1
+    big = R.params(buckets=(1 << 26) + 1, batch_size=4, num_batches=1)
+    assert L.ckt_hist_run(ctypes.byref(big), ckt.RED_LOCALIZE, 8, None, 0, None) == 1
+    assert b"localize" in L.ckt_last_error()
+    lo, hi = ctypes.c_uint64(), ctypes.c_uint64()
+    assert L.ckt_hist_scratch_bytes(ctypes.byref(p), ckt.RED_SINGLE, ctypes.byref(lo),
+                                    ctypes.byref(hi)) == 0 and lo.value == hi.value == 0
+    assert L.ckt_hist_scratch_bytes(ctypes.byref(p), ckt.RED_LIST, ctypes.byref(lo),
+                                    ctypes.byref(hi)) == 0 and lo.value == 32 and hi.value >= 32
+    wide = R.params(buckets=1 << 20, batch_size=4, num_batches=1)
+    assert L.ckt_hist_scratch_bytes(ctypes.byref(wide), ckt.RED_FOLD, ctypes.byref(lo),
+                                    ctypes.byref(hi)) == 0 and lo.value == 4 << 20
+    # too little scratch for a list: rejected before anything runs
+    assert L.ckt_hist_run(ctypes.byref(p), ckt.RED_LIST, 8, 16, 8, None) == 1
+    assert b"minimum" in L.ckt_last_error()

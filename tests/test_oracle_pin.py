@@ -114,3 +114,61 @@ def test_live_reference(oracle, tmp_path, args, loops):
     oracle.simulate(c, loops, 10000, quirk=True)
     for k in STATE:
         assert same_bits(getattr(c, k), getattr(final, k)), k
+
+
+# -- reduction microbenchmark (benchmarks/reductions/reducetest.cc) ---------------
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "hist_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_histogram_matches_reference(oracle, path):
+    """The reference's master histogram after its three default cases is
+    three times the oracle's histogram, bucket for bucket."""
+    g = load_npz(os.path.basename(path))
+    buckets, batches, bsize = (int(x) for x in g["params"])
+    h = oracle.histogram(buckets, bsize, batches)
+    assert h.sum() == batches * bsize
+    assert np.array_equal(g["master"], (h.astype(np.uint64) * int(g["cases"])).astype(np.uint32))
+
+
+def test_histogram_threads_equals_serial(oracle):
+    h = oracle.histogram(4099, 3000, 13)
+    for threads in (1, 2, 5, 16):
+        got, secs = oracle.histogram_threads(4099, 3000, 13, threads)
+        assert np.array_equal(got, h) and secs >= 0
+
+
+def test_histogram_first_batch_wraps_32_bits(oracle):
+    """Element indices are 32-bit unsigned like the benchmark's start + i:
+    batch 2**12 of 2**20 elements starts again at index 0."""
+    bs = 1 << 12
+    a = oracle.histogram(977, bs, 1, first_batch=(1 << 20))
+    b = oracle.histogram(977, bs, 1, first_batch=0)
+    assert np.array_equal(a, b)
+    # a batch straddling 2**32 equals its two halves
+    first = (1 << 32) // bs - 1
+    c = oracle.histogram(977, bs, 2, first_batch=first)
+    d = oracle.histogram(977, bs, 1, first_batch=first) + oracle.histogram(977, bs, 1)
+    assert np.array_equal(c, d)
+
+
+def test_hist_rand_known_values(oracle):
+    """myrand restated independently in Python (reducetest.cc:323-333)."""
+    def myrand(ival, s1, s2):
+        r = ival
+        for j in range(16):
+            r = (0x5DEECE66D * r + 0xB) & 0xFFFFFFFFFFFF
+            r ^= s1 if (ival >> j) & 1 else s2
+        return r & 0xFFFFFFFF
+
+    for ival in (0, 1, 2, 12345, 0xFFFF, 0x10000, 0xFFFFFFFF, 0x12345678):
+        assert oracle.lib().ocl_hist_rand(ival, 12345, 54321) == myrand(ival, 12345, 54321)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/benchmarks/reductions"),
+                    reason="reference tree absent")
+def test_histogram_live_reference(oracle, tmp_path):
+    oracle.build_ref()
+    for buckets, batches, bsize in [(3, 4, 1001), (100003, 2, 20000)]:
+        m = oracle.run_reducetest(buckets, batches, bsize, str(tmp_path / f"{buckets}"))
+        h = oracle.histogram(buckets, bsize, batches)
+        assert np.array_equal(m, (3 * h.astype(np.uint64)).astype(np.uint32))
