@@ -14,10 +14,16 @@ metric is wire-segment updates per second = wires x 10 segments x 1000
 inner steps x 10 loops / time.  The working set (411 MB of wire state) is
 larger than L2.
 
-  value  device-resident: state reset by a device copy, kernels on one stream
-  e2e    through the same C-ABI calls with host buffers: every step copies the
+  value  device-resident: state reset by a device copy, then per loop the
+         library's two fused launches (calc_new_currents with the charge
+         contributions as its epilogue, then one node pass for
+         distribute_charge + update_voltages; bit-identical to the three task
+         launches), on one stream
+  e2e    through ckt_run_loops_all with host buffers: every step copies the
          circuit from pinned host memory to the device, runs the 10 loops and
          copies the resulting state back
+  index_space_tasks  the same steps through the three separate index-space
+         task launches per loop (the drop-in boundary), with their kernels
 
 `--impl reference` times the reference's CPU implementation of the same three
 tasks (its shared-low-level execution style: one thread per core, piece p on
@@ -330,12 +336,20 @@ def main() -> None:
             for k in C.STATE_FIELDS:
                 dc.t[k].copy_(pristine[k], non_blocking=True)
 
-    kernel_events = {"cnc": [], "dc": [], "uv": []}
+    # The library's loop: calc_new_currents with the contribution scatter as
+    # its epilogue, then one node pass for distribute_charge +
+    # update_voltages (ckt_run_loops_all, bit-identical to the three task
+    # launches).  The three separate index-space launches -- the drop-in
+    # boundary -- are timed after it.
+    fused = (("cnc", lambda: L.ckt_calc_new_currents_scatter_all(g, w, n, ctypes.byref(prm), sp)),
+             ("dcuv", lambda: L.ckt_distribute_update_all(g, n, sp)))
+    tasks = (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
+             ("dc", lambda: L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), sp)),
+             ("uv", lambda: L.ckt_update_voltages_all(g, n, sp)))
+    kernel_events = {"cnc": [], "dcuv": [], "dc": [], "uv": []}
 
-    def loop(record: bool):
-        for name, fn in (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
-                         ("dc", lambda: L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), sp)),
-                         ("uv", lambda: L.ckt_update_voltages_all(g, n, sp))):
+    def loop(record: bool, calls=fused):
+        for name, fn in calls:
             if record:
                 a, b = E(), E()
                 a.record(stream)
@@ -345,10 +359,10 @@ def main() -> None:
             else:
                 G.check(fn())
 
-    def step(record: bool):
+    def step(record: bool, calls=fused):
         reset()
         for _ in range(OUTER_LOOPS):
-            loop(record)
+            loop(record, calls)
 
     def barrier():
         if dist is not None:
@@ -377,6 +391,24 @@ def main() -> None:
     launches = sum(len(v) for v in kernel_events.values())
     kt = {k: [a.elapsed_time(b) * 1e-3 for a, b in v] for k, v in kernel_events.items()}
 
+    # The drop-in boundary: the three index-space task launches per loop.
+    cnc_fused = kernel_events["cnc"]
+    kernel_events["cnc"] = []
+    task_steps = max(3, min(args.steps, 5))
+    for _ in range(args.warmup):
+        step(False, tasks)
+    torch.cuda.synchronize()
+    u0, u1 = E(), E()
+    u0.record(stream)
+    for _ in range(task_steps):
+        step(True, tasks)
+    u1.record(stream)
+    torch.cuda.synchronize()
+    tasks_value = updates_per_step * task_steps / (u0.elapsed_time(u1) * 1e-3)
+    kt_tasks = {k: [a.elapsed_time(b) * 1e-3 for a, b in kernel_events[k]]
+                for k in ("cnc", "dc", "uv")}
+    kernel_events["cnc"] = cnc_fused
+
     # Roofline of the dominant kernel (calc_new_currents, FP32-pipe bound).
     probe = fp32_peak(torch, G, stream)
     peak32 = probe["peak"]
@@ -388,7 +420,12 @@ def main() -> None:
     hbm = hbm or 6800.0
     dc_bytes = 16 * shape.W + 8 * shape.N
     uv_bytes = 24 * shape.N
-    dc_s, uv_s = statistics.mean(kt["dc"]), statistics.mean(kt["uv"])
+    # fused node pass: contributions 8 B per wire; per node the offset (4 B),
+    # charge, voltage, capacitance, leakage read (16 B), voltage and charge
+    # written (8 B)
+    dcuv_bytes = 8 * shape.W + 28 * shape.N
+    dc_s, uv_s = statistics.mean(kt_tasks["dc"]), statistics.mean(kt_tasks["uv"])
+    dcuv_s = statistics.mean(kt["dcuv"])
     roofline = {
         "kernel": "calc_new_currents", "bound": "fp32", "unit": "TFLOP/s",
         "achieved": cnc_flops / cnc_s / 1e12, "peak": peak32 / 1e12,
@@ -400,14 +437,27 @@ def main() -> None:
                        f"{INNER_STEPS} steps per launch",
         "traffic": None,
     }
+    cnc_task_s = statistics.mean(kt_tasks["cnc"])
     kernels = {
         "calc_new_currents": {"ms": 1e3 * cnc_s, "tflops": cnc_flops / cnc_s / 1e12,
-                              "frac_fp32_peak": cnc_flops / cnc_s / peak32},
+                              "frac_fp32_peak": cnc_flops / cnc_s / peak32,
+                              "note": "with the contribution scatter epilogue"},
+        "distribute_update": {"ms": 1e3 * dcuv_s, "algo_bytes": dcuv_bytes,
+                              "gbs": dcuv_bytes / dcuv_s / 1e9,
+                              "frac_hbm": dcuv_bytes / dcuv_s / 1e9 / hbm,
+                              "note": "distribute_charge + update_voltages in one node pass"},
+        "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
+    }
+    index_space_tasks = {
+        "value": tasks_value, "unit": UNIT, "steps": task_steps,
+        "note": "the three index-space task launches per loop (ckt_calc_new_currents_all, "
+                "ckt_distribute_charge_all, ckt_update_voltages_all)",
+        "calc_new_currents": {"ms": 1e3 * cnc_task_s,
+                              "frac_fp32_peak": cnc_flops / cnc_task_s / peak32},
         "distribute_charge": {"ms": 1e3 * dc_s, "algo_bytes": dc_bytes,
                               "gbs": dc_bytes / dc_s / 1e9, "frac_hbm": dc_bytes / dc_s / 1e9 / hbm},
         "update_voltages": {"ms": 1e3 * uv_s, "algo_bytes": uv_bytes,
                             "gbs": uv_bytes / uv_s / 1e9, "frac_hbm": uv_bytes / uv_s / 1e9 / hbm},
-        "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
     }
 
     # End to end through the same C-ABI calls with host buffers.
@@ -422,8 +472,7 @@ def main() -> None:
         with torch.cuda.stream(stream):
             for k in h2d_keys:
                 dc.t[k].copy_(pinned[k], non_blocking=True)
-        for _ in range(OUTER_LOOPS):
-            loop(False)
+        G.check(L.ckt_run_loops_all(g, w, n, ctypes.byref(prm), OUTER_LOOPS, sp))
         with torch.cuda.stream(stream):
             for k in C.STATE_FIELDS:
                 out_pinned[k].copy_(dc.t[k], non_blocking=True)
@@ -454,7 +503,7 @@ def main() -> None:
             "data": "synthetic (reference generator distributions, seed 12345)",
             "config": workload_config(args.mode, shape.num_pieces), "roofline": roofline,
             "cpu_baseline": cpu_baseline, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "kernels": kernels,
+            "clocks": clk.summary(), "kernels": kernels, "index_space_tasks": index_space_tasks,
             "replicas": "one independent circuit per GPU" if ws > 1 else None,
         }
         print(json.dumps(line), flush=True)

@@ -150,6 +150,12 @@ class DeviceCircuit:
         check(L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), stream))
         check(L.ckt_update_voltages_all(g, n, stream))
 
+    def run_loops(self, prm: Params, loops: int, stream: int = 0) -> None:
+        """`loops` outer loops fused across the task boundaries (two launches
+        per loop); bit-identical to `loops` calls of loop_index_space."""
+        check(lib().ckt_run_loops_all(self.graph.handle, self.wires(), self.nodes(),
+                                      ctypes.byref(prm), loops, stream))
+
     def loop_per_piece(self, prm: Params, stream: int = 0, blocking: bool = False) -> None:
         """One outer loop as the reference's per-piece task calls: CNC for
         every piece; DC for every piece, each followed by the application of

@@ -129,6 +129,45 @@ def test_per_piece_calls_equal_index_space(cuda, oracle, shape):
         assert same_bits(a[k], getattr(c, k)), k
 
 
+@pytest.mark.parametrize("shape", sorted(SHAPES))
+@pytest.mark.parametrize("mode,init", [(0, 0), (1, 0), (2, 0), (0, 1)])
+def test_fused_loops_equal_index_space(cuda, oracle, shape, mode, init):
+    """ckt_run_loops_all (contributions scattered by calc_new_currents, one
+    node pass for distribute_charge + update_voltages) gives the bits of the
+    three index-space launches per loop."""
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(*SHAPES[shape], L_offset=0.001))
+    a_dev, b_dev = device(cuda, c), device(cuda, c)
+    prm = C.params(3, mode, init)
+    a_dev.run_loops(prm, 4)
+    for _ in range(4):
+        b_dev.loop_index_space(prm)
+    cuda.cuda.synchronize()
+    a, b = a_dev.to_host(), b_dev.to_host()
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), (shape, k)
+    if mode == 0 and init == 0:
+        oracle.simulate(c, 4, 3)
+        for k in STATE:
+            assert same_bits(a[k], getattr(c, k)), (shape, k)
+
+
+def test_fused_loops_without_wires(cuda, oracle):
+    """No wires: every loop is the voltage update alone."""
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(3, 4, 0, 95, 1, L_offset=0.001))
+    c.charge[:] = np.linspace(-1, 1, c.charge.size, dtype=np.float32)
+    dev = device(cuda, c)
+    dev.run_loops(C.params(5, 0), 2)
+    cuda.cuda.synchronize()
+    got = dev.to_host()
+    oracle.simulate(c, 2, 5)
+    for k in STATE:
+        assert same_bits(got[k], getattr(c, k)), k
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_blocking_task_forms_equal_async(cuda, oracle, mode):
     """ckt_*_sync (a device wait after every task, like the reference's GPU
