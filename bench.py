@@ -15,8 +15,7 @@ inner steps x 10 loops / time.  The working set (411 MB of wire state) is
 larger than L2.
 
   value  device-resident: state reset by a device copy, then per loop the
-         library's two fused launches (calc_new_currents with the charge
-         contributions as its epilogue, then one node pass for
+         library's two launches (calc_new_currents, then one node pass for
          distribute_charge + update_voltages; bit-identical to the three task
          launches), on one stream
   e2e    through ckt_run_loops_all with host buffers: every step copies the
@@ -336,13 +335,12 @@ def main() -> None:
             for k in C.STATE_FIELDS:
                 dc.t[k].copy_(pristine[k], non_blocking=True)
 
-    # The library's loop: calc_new_currents with the contribution scatter as
-    # its epilogue, then one node pass for distribute_charge +
-    # update_voltages (ckt_run_loops_all, bit-identical to the three task
-    # launches).  The three separate index-space launches -- the drop-in
-    # boundary -- are timed after it.
-    fused = (("cnc", lambda: L.ckt_calc_new_currents_scatter_all(g, w, n, ctypes.byref(prm), sp)),
-             ("dcuv", lambda: L.ckt_distribute_update_all(g, n, sp)))
+    # The library's loop: calc_new_currents, then one node pass for
+    # distribute_charge + update_voltages (ckt_run_loops_all, bit-identical
+    # to the three task launches).  The three separate index-space launches
+    # -- the drop-in boundary -- are timed after it.
+    fused = (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
+             ("dcuv", lambda: L.ckt_distribute_update_all(g, w, n, ctypes.byref(prm), sp)))
     tasks = (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
              ("dc", lambda: L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), sp)),
              ("uv", lambda: L.ckt_update_voltages_all(g, n, sp)))
@@ -420,10 +418,9 @@ def main() -> None:
     hbm = hbm or 6800.0
     dc_bytes = 16 * shape.W + 8 * shape.N
     uv_bytes = 24 * shape.N
-    # fused node pass: contributions 8 B per wire; per node the offset (4 B),
-    # charge, voltage, capacitance, leakage read (16 B), voltage and charge
-    # written (8 B)
-    dcuv_bytes = 8 * shape.W + 28 * shape.N
+    # fused node pass: the two tasks' bytes (16 W + 8 N and 24 N) less the
+    # charge written by one and read by the other (8 N)
+    dcuv_bytes = 16 * shape.W + 24 * shape.N
     dc_s, uv_s = statistics.mean(kt_tasks["dc"]), statistics.mean(kt_tasks["uv"])
     dcuv_s = statistics.mean(kt["dcuv"])
     roofline = {
@@ -440,8 +437,7 @@ def main() -> None:
     cnc_task_s = statistics.mean(kt_tasks["cnc"])
     kernels = {
         "calc_new_currents": {"ms": 1e3 * cnc_s, "tflops": cnc_flops / cnc_s / 1e12,
-                              "frac_fp32_peak": cnc_flops / cnc_s / peak32,
-                              "note": "with the contribution scatter epilogue"},
+                              "frac_fp32_peak": cnc_flops / cnc_s / peak32},
         "distribute_update": {"ms": 1e3 * dcuv_s, "algo_bytes": dcuv_bytes,
                               "gbs": dcuv_bytes / dcuv_s / 1e9,
                               "frac_hbm": dcuv_bytes / dcuv_s / 1e9 / hbm,

@@ -226,25 +226,16 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
                               const ckt_params *prm, void *stream);
 int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *stream);
 
-/* The outer loop fused across the task boundaries (no counterpart in the
- * reference, whose tasks meet only through region instances):
- *  - ckt_calc_new_currents_scatter_all is ckt_calc_new_currents_all that
- *    also stores each wire's two charge contributions, -dt*I[0] and dt*I[9],
- *    in the graph's contribution buffer at the CSR positions of its ends;
- *  - ckt_distribute_update_all is ckt_distribute_charge_all followed by
- *    ckt_update_voltages_all, reading the contributions the last scatter
- *    call on this graph stored (stream order) instead of the currents: one
- *    contiguous pass that sums every node's run in the reference order and
- *    feeds the sum straight into the voltage update;
- *  - ckt_run_loops_all runs `loops` outer loops of region_main
- *    (apps/circuit/circuit.cc:232-307) as those two calls per loop.
- * Bit-identical to the same loops of ckt_calc_new_currents_all,
- * ckt_distribute_charge_all and ckt_update_voltages_all.  The contribution
- * buffer belongs to the graph: calls on one graph must not overlap on the
- * GPU. */
-int ckt_calc_new_currents_scatter_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
-                                      const ckt_params *prm, void *stream);
-int ckt_distribute_update_all(const ckt_graph *graph, ckt_nodes nodes, void *stream);
+/* distribute_charge and update_voltages over all pieces fused into one node
+ * pass (no counterpart in the reference, whose tasks meet only through
+ * region instances): each node gathers its contributions as
+ * ckt_distribute_charge_all does and feeds the sum straight into the
+ * voltage update.  Bit-identical to ckt_distribute_charge_all followed by
+ * ckt_update_voltages_all.  ckt_run_loops_all runs `loops` outer loops of
+ * region_main (apps/circuit/circuit.cc:232-307) as ckt_calc_new_currents_all
+ * plus this pass: two launches per loop instead of three. */
+int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream);
 int ckt_run_loops_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                       const ckt_params *prm, int32_t loops, void *stream);
 

@@ -151,8 +151,9 @@ class DeviceCircuit:
         check(L.ckt_update_voltages_all(g, n, stream))
 
     def run_loops(self, prm: Params, loops: int, stream: int = 0) -> None:
-        """`loops` outer loops fused across the task boundaries (two launches
-        per loop); bit-identical to `loops` calls of loop_index_space."""
+        """`loops` outer loops with distribute_charge and update_voltages
+        fused into one node pass (two launches per loop); bit-identical to
+        `loops` calls of loop_index_space."""
         check(lib().ckt_run_loops_all(self.graph.handle, self.wires(), self.nodes(),
                                       ctypes.byref(prm), loops, stream))
 

@@ -232,23 +232,6 @@ __global__ void __launch_bounds__(256)
   cnc_wire<MODE, INIT>((int64_t)first_wire + t, a, v, steps, dt);
 }
 
-// calc_new_currents of the fused loop: the same wire update, then the wire's
-// two distribute_charge contributions, -dt*I[0] and dt*I[9]
-// (apps/circuit/circuit.cc:430-431), stored at the CSR positions of its two
-// ends, so the node pass reads them contiguously.
-template <int MODE, int INIT>
-__global__ void __launch_bounds__(256)
-    cnc_scatter_kernel(uint32_t num_wires, WireArrays a, NodeVolts v, int steps, float dt,
-                       const uint32_t *__restrict__ slot_in,
-                       const uint32_t *__restrict__ slot_out, float *__restrict__ contrib) {
-  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= num_wires) return;
-  float i0, i9;
-  cnc_wire<MODE, INIT>((int64_t)w, a, v, steps, dt, &i0, &i9);
-  contrib[slot_in[w]] = __fmul_rn(-dt, i0);
-  contrib[slot_out[w]] = __fmul_rn(dt, i9);
-}
-
 // ---------------------------------------------------------------------------
 // distribute_charge.  The reference adds -dt*I[0] to the in-node and
 // +dt*I[9] to the out-node of every wire with atomicAdd (unordered).  Here
@@ -279,8 +262,10 @@ __device__ __forceinline__ float ld_f32(const float *p) {
   return COHERENT ? __ldcg(p) : *p;
 }
 
-template <uint32_t BLOCK, bool COHERENT>
-__device__ __forceinline__ void dc_block(uint32_t x0, uint32_t xe,
+// Returns the thread's node's new charge; STORE = false leaves charge[]
+// unwritten for a caller that consumes the value itself.
+template <uint32_t BLOCK, bool COHERENT, bool STORE = true>
+__device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
                                          const uint32_t *__restrict__ off,
                                          const uint32_t *__restrict__ ent,
                                          const float *__restrict__ I0,
@@ -344,8 +329,9 @@ __device__ __forceinline__ void dc_block(uint32_t x0, uint32_t xe,
   }
   if (x < xe) {
     if (!priv && e > b) acc = __fadd_rn(acc, fold);
-    charge[x] = acc;
+    if (STORE) charge[x] = acc;
   }
+  return acc;
 }
 
 // The simple schedule: one thread per node walks its own run with dependent
@@ -539,56 +525,30 @@ static __global__ void __launch_bounds__(256)
   s.charge[x] = 0.0f;
 }
 
-// distribute_charge + update_voltages of the fused loop, a block per 256
-// nodes.  The block's contributions are one contiguous span of the
-// contribution buffer: staged with coalesced loads, summed per node in the
-// reference order (as dc_sum_kernel), and the node's final charge goes
-// straight into the voltage update (uv_one) instead of through memory.
-static __global__ void __launch_bounds__(256)
-    dcuv_kernel(uint32_t N, const uint32_t *__restrict__ off, const float *__restrict__ contrib,
-                const uint32_t *__restrict__ gstart, float *__restrict__ charge,
-                float *__restrict__ voltage, const float *__restrict__ cap,
-                const float *__restrict__ leak) {
+// distribute_charge + update_voltages in one node pass (the fused loop): the
+// staged gather of dc_block, and each node's final charge goes straight into
+// the voltage update instead of through memory.  Same order, same bits as
+// dc_all_kernel followed by the update_voltages kernels.
+static __global__ void __launch_bounds__(kDcBlock)
+    dcuv_kernel(uint32_t N, const uint32_t *__restrict__ off, const uint32_t *__restrict__ ent,
+                const float *__restrict__ I0, const float *__restrict__ I9,
+                float *__restrict__ charge, float *__restrict__ voltage,
+                const float *__restrict__ cap, const float *__restrict__ leak, float dt) {
   __shared__ float sval[kDcChunk];
-  const uint32_t x0 = blockIdx.x * 256u;
-  const uint32_t xe = min(N, x0 + 256u);
+  __shared__ uint8_t sflag[kDcChunk];
+  const uint32_t x0 = blockIdx.x * kDcBlock;
+  const uint32_t xe = min(N, x0 + kDcBlock);
   const uint32_t x = x0 + threadIdx.x;
-  const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
-  uint32_t b = 0, e = 0;
-  bool priv = true;
-  float acc = 0.0f, fold = 0.0f, v = 0.0f, c = 1.0f, l = 0.0f;
-  if (x < xe) {
-    const uint32_t o0 = off[x], o1 = off[x + 1];
-    priv = (o0 & 0x80000000u) != 0;
-    b = o0 & 0x7fffffffu;
-    e = o1 & 0x7fffffffu;
-    acc = charge[x];
+  float v = 0.0f, c = 1.0f, l = 0.0f;
+  if (x < xe) {  // independent of the gather: in flight while it runs
     v = voltage[x];
     c = cap[x];
     l = leak[x];
   }
-  for (uint32_t c0 = lo; c0 < hi; c0 += kDcChunk) {
-    const uint32_t cn = min(kDcChunk, hi - c0);
-#pragma unroll 8
-    for (uint32_t j = threadIdx.x; j < cn; j += 256u) sval[j] = __ldcs(contrib + c0 + j);
-    __syncthreads();
-    const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
-    if (priv) {
-      for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sval[i - c0]);
-    } else {
-      for (uint32_t i = i0; i < i1; i++) {
-        if (i != b && ((gstart[i >> 5] >> (i & 31u)) & 1u)) {
-          acc = __fadd_rn(acc, fold);
-          fold = 0.0f;
-        }
-        fold = __fadd_rn(fold, sval[i - c0]);
-      }
-    }
-    __syncthreads();
-  }
+  const float q = dc_block<kDcBlock, false, false>(x0, xe, off, ent, I0, I9, charge, dt, sval,
+                                                  sflag);
   if (x < xe) {
-    if (!priv && e > b) acc = __fadd_rn(acc, fold);
-    voltage[x] = uv_one(v, acc, c, l);
+    voltage[x] = uv_one(v, q, c, l);
     charge[x] = 0.0f;
   }
 }

@@ -279,46 +279,18 @@ int ckt_update_voltages_sync(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes sh
   return rc ? rc : wait_stream(stream, "update_voltages");
 }
 
-int ckt_calc_new_currents_scatter_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
-                                      const ckt_params *prm, void *stream) {
+int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                              const ckt_params *prm, void *stream) {
   int rc;
   CKT_REQUIRE(graph != nullptr, "graph is NULL");
-  if ((rc = validate_params(prm))) return rc;
-  if (graph->W == 0) return CKT_OK;
-  if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
-  CKT_REQUIRE(nodes.voltage != nullptr, "node voltage array is NULL");
-  const cudaStream_t s = as_stream(stream);
-  const uint32_t W = (uint32_t)graph->W;
-  const WireArrays a = wire_arrays(wires);
-  const NodeVolts v = {nodes.voltage, nodes.voltage, nodes.voltage};
-#define CKT_SCATTER(M, I)                                                                   \
-  cnc_scatter_kernel<M, I><<<grid_for(W), 256, 0, s>>>(W, a, v, prm->steps, prm->dt,        \
-                                                        graph->slot_in, graph->slot_out,    \
-                                                        graph->contrib)
-  if (prm->mode == CKT_MODE_EXACT) {
-    if (prm->init == CKT_INIT_KERNEL) CKT_SCATTER(CKT_MODE_EXACT, CKT_INIT_KERNEL);
-    else CKT_SCATTER(CKT_MODE_EXACT, CKT_INIT_CPU_TASK);
-  } else if (prm->mode == CKT_MODE_FAST) {
-    if (prm->init == CKT_INIT_KERNEL) CKT_SCATTER(CKT_MODE_FAST, CKT_INIT_KERNEL);
-    else CKT_SCATTER(CKT_MODE_FAST, CKT_INIT_CPU_TASK);
-  } else {
-    if (prm->init == CKT_INIT_KERNEL) CKT_SCATTER(kModeFastScalar, CKT_INIT_KERNEL);
-    else CKT_SCATTER(kModeFastScalar, CKT_INIT_CPU_TASK);
-  }
-#undef CKT_SCATTER
-  CKT_CHECK_LAUNCH();
-  return CKT_OK;
-}
-
-int ckt_distribute_update_all(const ckt_graph *graph, ckt_nodes nodes, void *stream) {
-  int rc;
-  CKT_REQUIRE(graph != nullptr, "graph is NULL");
-  if ((rc = validate_nodes(nodes, "nodes"))) return rc;
+  if ((rc = validate_params(prm)) || (rc = validate_nodes(nodes, "nodes"))) return rc;
   if (graph->N == 0) return CKT_OK;
-  const uint32_t N = (uint32_t)graph->N;
-  dcuv_kernel<<<grid_for(N), 256, 0, as_stream(stream)>>>(
-      N, graph->node_off, graph->contrib, graph->gstart, nodes.charge, nodes.voltage,
-      nodes.capacitance, nodes.leakage);
+  if (graph->W == 0) return ckt_update_voltages_all(graph, nodes, stream);
+  if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
+  const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
+  dcuv_kernel<<<grid_for(graph->N, kDcBlock), kDcBlock, 0, as_stream(stream)>>>(
+      (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, nodes.voltage,
+      nodes.capacitance, nodes.leakage, prm->dt);
   CKT_CHECK_LAUNCH();
   return CKT_OK;
 }
@@ -330,8 +302,8 @@ int ckt_run_loops_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
   if ((rc = validate_params(prm)) || (rc = validate_nodes(nodes, "nodes"))) return rc;
   CKT_REQUIRE(loops >= 0, "loops must be >= 0 (got %d)", loops);
   for (int32_t l = 0; l < loops; l++) {
-    if ((rc = ckt_calc_new_currents_scatter_all(graph, wires, nodes, prm, stream)) ||
-        (rc = ckt_distribute_update_all(graph, nodes, stream)))
+    if ((rc = ckt_calc_new_currents_all(graph, wires, nodes, prm, stream)) ||
+        (rc = ckt_distribute_update_all(graph, wires, nodes, prm, stream)))
       return rc;
   }
   return CKT_OK;
