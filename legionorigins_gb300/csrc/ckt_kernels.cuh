@@ -126,6 +126,33 @@ struct PackedFast {
   }
 };
 
+// FAST, two wires per thread: wire a's segment k and wire b's segment k
+// share every paired instruction, so all 58 operations of a wire-step pair
+// up with no cross-lane moves (29 instructions per wire-step).  Each lane is
+// rounded exactly as the scalar step: bit-identical to it.
+struct DualFast {
+  float2 nLdt, rR, dtC, neg1;
+  __device__ __forceinline__ DualFast(float2 l, float2 r, float2 c, float d) {
+    const FastConsts ka(l.x, r.x, c.x, d), kb(l.y, r.y, c.y, d);
+    nLdt = make_float2(ka.nLdt, kb.nLdt);
+    rR = make_float2(ka.rR, kb.rR);
+    dtC = make_float2(ka.dtC, kb.dtC);
+    neg1 = make_float2(-1.0f, -1.0f);
+  }
+  // ni[k] = (i_k of a, i_k of b), nv[k] likewise; nI0 = -I0; V0 = wire voltages.
+  __device__ __forceinline__ void step(float2 (&ni)[10], float2 (&nv)[11], const float2 (&nI0)[10],
+                                       const float2 (&V0)[9]) const {
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      const float2 dv = __ffma2_rn(nv[k], neg1, nv[k + 1]);
+      const float2 di = __fadd2_rn(ni[k], nI0[k]);
+      ni[k] = __fmul2_rn(__ffma2_rn(nLdt, di, dv), rR);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k + 1] = __ffma2_rn(dtC, __ffma2_rn(ni[k + 1], neg1, ni[k]), V0[k]);
+  }
+};
+
 __device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *pvt,
                                                       const float *shr, const float *ghost) {
   // get_node (apps/circuit/circuit_gpu.cu:40-59) without its assert: a
@@ -221,6 +248,71 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
   for (int k = 0; k < 9; k++) a.vol[k * S + w] = nv[k + 1];
   if (i0_out) *i0_out = ni[0];
   if (i9_out) *i9_out = ni[9];
+}
+
+// FAST mode, two wires per thread (DualFast): thread t of a block handles
+// wires base + t and base + t + 256, so each field's loads and stores stay
+// one contiguous line per warp.  Without a partner wire the thread runs its
+// wire in both lanes and stores one.
+template <int INIT>
+__device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b,
+                                              const WireArrays &a, const NodeVolts &nvin,
+                                              int steps, float dt) {
+  const int64_t S = a.S;
+  float2 ni[10], nI0[10], nv[11], V0[9];
+#pragma unroll
+  for (int k = 0; k < 10; k++) {
+    const float x = a.cur[k * S + wa], y = a.cur[k * S + wb];
+    ni[k] = make_float2(x, y);
+    nI0[k] = make_float2(-x, -y);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) V0[k] = make_float2(a.vol[k * S + wa], a.vol[k * S + wb]);
+  const float out_a = pick_instance(a.out_loc[wa], nvin.pvt, nvin.shr, nvin.ghost)[a.out_ptr[wa]];
+  const float out_b = pick_instance(a.out_loc[wb], nvin.pvt, nvin.shr, nvin.ghost)[a.out_ptr[wb]];
+  if (INIT == CKT_INIT_KERNEL) {
+    nv[0] = make_float2(pick_instance(a.in_loc[wa], nvin.pvt, nvin.shr, nvin.ghost)[a.in_ptr[wa]],
+                        pick_instance(a.in_loc[wb], nvin.pvt, nvin.shr, nvin.ghost)[a.in_ptr[wb]]);
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k + 1] = V0[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k] = V0[k];
+    nv[9] = make_float2(0.0f, 0.0f);
+  }
+  nv[10] = make_float2(out_a, out_b);
+  const DualFast pk(make_float2(a.L[wa], a.L[wb]), make_float2(a.R[wa], a.R[wb]),
+                    make_float2(a.C[wa], a.C[wb]), dt);
+  int j = 0;
+#pragma unroll 1
+  for (; j + 2 <= steps; j += 2) {
+    pk.step(ni, nv, nI0, V0);
+    pk.step(ni, nv, nI0, V0);
+  }
+  if (j < steps) pk.step(ni, nv, nI0, V0);
+#pragma unroll
+  for (int k = 0; k < 10; k++) a.cur[k * S + wa] = ni[k].x;
+#pragma unroll
+  for (int k = 0; k < 9; k++) a.vol[k * S + wa] = nv[k + 1].x;
+  if (has_b) {
+#pragma unroll
+    for (int k = 0; k < 10; k++) a.cur[k * S + wb] = ni[k].y;
+#pragma unroll
+    for (int k = 0; k < 9; k++) a.vol[k * S + wb] = nv[k + 1].y;
+  }
+}
+
+constexpr int kPairBlock = 256;  // threads; a block covers 2 * kPairBlock wires
+
+template <int INIT>
+__global__ void __launch_bounds__(kPairBlock)
+    cnc_pair_kernel(uint32_t first_wire, uint32_t num_wires, WireArrays a, NodeVolts v, int steps,
+                    float dt) {
+  const uint32_t ta = blockIdx.x * (2 * kPairBlock) + threadIdx.x, tb = ta + kPairBlock;
+  if (ta >= num_wires) return;
+  const bool has_b = tb < num_wires;
+  cnc_wire_pair<INIT>((int64_t)first_wire + ta, (int64_t)first_wire + (has_b ? tb : ta), has_b,
+                      a, v, steps, dt);
 }
 
 template <int MODE, int INIT>
@@ -334,6 +426,74 @@ __device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
   return acc;
 }
 
+// Whole circuit, canonical order, a warp per 32 consecutive nodes: the warp
+// stages its span of the CSR in chunks of kDcWarpChunk entries (16
+// coalesced entry loads and 16 independent current gathers per lane), then
+// each lane sums its node's run.  No block barrier: warps progress
+// independently, which measured faster than the block-staged dc_block for
+// the whole-circuit launch.  Same order, same bits.
+constexpr uint32_t kDcWarpChunk = 512;
+
+__device__ __forceinline__ float dc_warp(uint32_t x0, uint32_t xe, const uint32_t *__restrict__ off,
+                                         const uint32_t *__restrict__ ent,
+                                         const float *__restrict__ I0,
+                                         const float *__restrict__ I9,
+                                         const float *__restrict__ charge, float dt, float *sv,
+                                         uint8_t *sf) {
+  const uint32_t lane = threadIdx.x & 31u, x = x0 + lane;
+  const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
+  uint32_t b = 0, e = 0;
+  bool priv = true;
+  float acc = 0.0f, fold = 0.0f;
+  if (x < xe) {
+    const uint32_t o0 = off[x], o1 = off[x + 1];
+    priv = (o0 & 0x80000000u) != 0;
+    b = o0 & 0x7fffffffu;
+    e = o1 & 0x7fffffffu;
+    acc = charge[x];
+  }
+  constexpr uint32_t K = kDcWarpChunk / 32;
+  for (uint32_t c0 = lo; c0 < hi; c0 += kDcWarpChunk) {
+    const uint32_t cn = min(kDcWarpChunk, hi - c0);
+    uint32_t u[K];
+#pragma unroll
+    for (uint32_t r = 0; r < K; r++) {
+      const uint32_t j = r * 32 + lane;
+      u[r] = j < cn ? ent[c0 + j] : 0u;
+    }
+    float v[K];
+#pragma unroll
+    for (uint32_t r = 0; r < K; r++) {
+      const uint32_t j = r * 32 + lane, w = u[r] >> 2;
+      v[r] = j < cn ? ((u[r] & 2u) ? I9[w] : I0[w]) : 0.0f;
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < K; r++) {
+      const uint32_t j = r * 32 + lane;
+      if (j < cn) {
+        sv[j] = (u[r] & 2u) ? __fmul_rn(dt, v[r]) : __fmul_rn(-dt, v[r]);
+        sf[j] = (uint8_t)(u[r] & 1u);
+      }
+    }
+    __syncwarp();
+    const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
+    if (priv) {
+      for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sv[i - c0]);
+    } else {
+      for (uint32_t i = i0; i < i1; i++) {
+        if (sf[i - c0] && i != b) {
+          acc = __fadd_rn(acc, fold);
+          fold = 0.0f;
+        }
+        fold = __fadd_rn(fold, sv[i - c0]);
+      }
+    }
+    __syncwarp();
+  }
+  if (x < xe && !priv && e > b) acc = __fadd_rn(acc, fold);
+  return acc;
+}
+
 // The simple schedule: one thread per node walks its own run with dependent
 // loads (no staging).  Same order, same bits.
 template <bool COHERENT>
@@ -434,11 +594,14 @@ static __global__ void __launch_bounds__(kDcBlock)
     dc_all_kernel(uint32_t node_begin, uint32_t node_end, const uint32_t *__restrict__ off,
                   const uint32_t *__restrict__ ent, const float *__restrict__ I0,
                   const float *__restrict__ I9, float *__restrict__ charge, float dt) {
-  __shared__ float sval[kDcChunk];
-  __shared__ uint8_t sflag[kDcChunk];
-  const uint32_t x0 = node_begin + blockIdx.x * kDcBlock;
-  dc_block<kDcBlock, false>(x0, min(node_end, x0 + kDcBlock), off, ent, I0, I9, charge, dt, sval,
-                            sflag);
+  __shared__ float sval[kDcBlock / 32][kDcWarpChunk];
+  __shared__ uint8_t sflag[kDcBlock / 32][kDcWarpChunk];
+  const uint32_t wp = threadIdx.x >> 5;
+  const uint32_t x0 = node_begin + blockIdx.x * kDcBlock + wp * 32u;
+  if (x0 >= node_end) return;
+  const uint32_t xe = min(node_end, x0 + 32u), x = x0 + (threadIdx.x & 31u);
+  const float q = dc_warp(x0, xe, off, ent, I0, I9, charge, dt, sval[wp], sflag[wp]);
+  if (x < xe) charge[x] = q;
 }
 
 // One piece: one thread per node the piece touches; private nodes are
@@ -526,7 +689,7 @@ static __global__ void __launch_bounds__(256)
 }
 
 // distribute_charge + update_voltages in one node pass (the fused loop): the
-// staged gather of dc_block, and each node's final charge goes straight into
+// warp-staged gather of dc_warp, and each node's final charge goes straight into
 // the voltage update instead of through memory.  Same order, same bits as
 // dc_all_kernel followed by the update_voltages kernels.
 static __global__ void __launch_bounds__(kDcBlock)
@@ -534,19 +697,19 @@ static __global__ void __launch_bounds__(kDcBlock)
                 const float *__restrict__ I0, const float *__restrict__ I9,
                 float *__restrict__ charge, float *__restrict__ voltage,
                 const float *__restrict__ cap, const float *__restrict__ leak, float dt) {
-  __shared__ float sval[kDcChunk];
-  __shared__ uint8_t sflag[kDcChunk];
-  const uint32_t x0 = blockIdx.x * kDcBlock;
-  const uint32_t xe = min(N, x0 + kDcBlock);
-  const uint32_t x = x0 + threadIdx.x;
+  __shared__ float sval[kDcBlock / 32][kDcWarpChunk];
+  __shared__ uint8_t sflag[kDcBlock / 32][kDcWarpChunk];
+  const uint32_t wp = threadIdx.x >> 5;
+  const uint32_t x0 = blockIdx.x * kDcBlock + wp * 32u;
+  if (x0 >= N) return;
+  const uint32_t xe = min(N, x0 + 32u), x = x0 + (threadIdx.x & 31u);
   float v = 0.0f, c = 1.0f, l = 0.0f;
   if (x < xe) {  // independent of the gather: in flight while it runs
     v = voltage[x];
     c = cap[x];
     l = leak[x];
   }
-  const float q = dc_block<kDcBlock, false, false>(x0, xe, off, ent, I0, I9, charge, dt, sval,
-                                                  sflag);
+  const float q = dc_warp(x0, xe, off, ent, I0, I9, charge, dt, sval[wp], sflag[wp]);
   if (x < xe) {
     voltage[x] = uv_one(v, q, c, l);
     charge[x] = 0.0f;
