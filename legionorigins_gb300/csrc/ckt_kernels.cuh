@@ -426,74 +426,6 @@ __device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
   return acc;
 }
 
-// Whole circuit, canonical order, a warp per 32 consecutive nodes: the warp
-// stages its span of the CSR in chunks of kDcWarpChunk entries (16
-// coalesced entry loads and 16 independent current gathers per lane), then
-// each lane sums its node's run.  No block barrier: warps progress
-// independently, which measured faster than the block-staged dc_block for
-// the whole-circuit launch.  Same order, same bits.
-constexpr uint32_t kDcWarpChunk = 512;
-
-__device__ __forceinline__ float dc_warp(uint32_t x0, uint32_t xe, const uint32_t *__restrict__ off,
-                                         const uint32_t *__restrict__ ent,
-                                         const float *__restrict__ I0,
-                                         const float *__restrict__ I9,
-                                         const float *__restrict__ charge, float dt, float *sv,
-                                         uint8_t *sf) {
-  const uint32_t lane = threadIdx.x & 31u, x = x0 + lane;
-  const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
-  uint32_t b = 0, e = 0;
-  bool priv = true;
-  float acc = 0.0f, fold = 0.0f;
-  if (x < xe) {
-    const uint32_t o0 = off[x], o1 = off[x + 1];
-    priv = (o0 & 0x80000000u) != 0;
-    b = o0 & 0x7fffffffu;
-    e = o1 & 0x7fffffffu;
-    acc = charge[x];
-  }
-  constexpr uint32_t K = kDcWarpChunk / 32;
-  for (uint32_t c0 = lo; c0 < hi; c0 += kDcWarpChunk) {
-    const uint32_t cn = min(kDcWarpChunk, hi - c0);
-    uint32_t u[K];
-#pragma unroll
-    for (uint32_t r = 0; r < K; r++) {
-      const uint32_t j = r * 32 + lane;
-      u[r] = j < cn ? ent[c0 + j] : 0u;
-    }
-    float v[K];
-#pragma unroll
-    for (uint32_t r = 0; r < K; r++) {
-      const uint32_t j = r * 32 + lane, w = u[r] >> 2;
-      v[r] = j < cn ? ((u[r] & 2u) ? I9[w] : I0[w]) : 0.0f;
-    }
-#pragma unroll
-    for (uint32_t r = 0; r < K; r++) {
-      const uint32_t j = r * 32 + lane;
-      if (j < cn) {
-        sv[j] = (u[r] & 2u) ? __fmul_rn(dt, v[r]) : __fmul_rn(-dt, v[r]);
-        sf[j] = (uint8_t)(u[r] & 1u);
-      }
-    }
-    __syncwarp();
-    const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
-    if (priv) {
-      for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sv[i - c0]);
-    } else {
-      for (uint32_t i = i0; i < i1; i++) {
-        if (sf[i - c0] && i != b) {
-          acc = __fadd_rn(acc, fold);
-          fold = 0.0f;
-        }
-        fold = __fadd_rn(fold, sv[i - c0]);
-      }
-    }
-    __syncwarp();
-  }
-  if (x < xe && !priv && e > b) acc = __fadd_rn(acc, fold);
-  return acc;
-}
-
 // The simple schedule: one thread per node walks its own run with dependent
 // loads (no staging).  Same order, same bits.
 template <bool COHERENT>
@@ -594,14 +526,11 @@ static __global__ void __launch_bounds__(kDcBlock)
     dc_all_kernel(uint32_t node_begin, uint32_t node_end, const uint32_t *__restrict__ off,
                   const uint32_t *__restrict__ ent, const float *__restrict__ I0,
                   const float *__restrict__ I9, float *__restrict__ charge, float dt) {
-  __shared__ float sval[kDcBlock / 32][kDcWarpChunk];
-  __shared__ uint8_t sflag[kDcBlock / 32][kDcWarpChunk];
-  const uint32_t wp = threadIdx.x >> 5;
-  const uint32_t x0 = node_begin + blockIdx.x * kDcBlock + wp * 32u;
-  if (x0 >= node_end) return;
-  const uint32_t xe = min(node_end, x0 + 32u), x = x0 + (threadIdx.x & 31u);
-  const float q = dc_warp(x0, xe, off, ent, I0, I9, charge, dt, sval[wp], sflag[wp]);
-  if (x < xe) charge[x] = q;
+  __shared__ float sval[kDcChunk];
+  __shared__ uint8_t sflag[kDcChunk];
+  const uint32_t x0 = node_begin + blockIdx.x * kDcBlock;
+  dc_block<kDcBlock, false>(x0, min(node_end, x0 + kDcBlock), off, ent, I0, I9, charge, dt, sval,
+                            sflag);
 }
 
 // One piece: one thread per node the piece touches; private nodes are
@@ -689,7 +618,7 @@ static __global__ void __launch_bounds__(256)
 }
 
 // distribute_charge + update_voltages in one node pass (the fused loop): the
-// warp-staged gather of dc_warp, and each node's final charge goes straight into
+// staged gather of dc_block, and each node's final charge goes straight into
 // the voltage update instead of through memory.  Same order, same bits as
 // dc_all_kernel followed by the update_voltages kernels.
 static __global__ void __launch_bounds__(kDcBlock)
@@ -697,19 +626,19 @@ static __global__ void __launch_bounds__(kDcBlock)
                 const float *__restrict__ I0, const float *__restrict__ I9,
                 float *__restrict__ charge, float *__restrict__ voltage,
                 const float *__restrict__ cap, const float *__restrict__ leak, float dt) {
-  __shared__ float sval[kDcBlock / 32][kDcWarpChunk];
-  __shared__ uint8_t sflag[kDcBlock / 32][kDcWarpChunk];
-  const uint32_t wp = threadIdx.x >> 5;
-  const uint32_t x0 = blockIdx.x * kDcBlock + wp * 32u;
-  if (x0 >= N) return;
-  const uint32_t xe = min(N, x0 + 32u), x = x0 + (threadIdx.x & 31u);
+  __shared__ float sval[kDcChunk];
+  __shared__ uint8_t sflag[kDcChunk];
+  const uint32_t x0 = blockIdx.x * kDcBlock;
+  const uint32_t xe = min(N, x0 + kDcBlock);
+  const uint32_t x = x0 + threadIdx.x;
   float v = 0.0f, c = 1.0f, l = 0.0f;
   if (x < xe) {  // independent of the gather: in flight while it runs
     v = voltage[x];
     c = cap[x];
     l = leak[x];
   }
-  const float q = dc_warp(x0, xe, off, ent, I0, I9, charge, dt, sval[wp], sflag[wp]);
+  const float q = dc_block<kDcBlock, false, false>(x0, xe, off, ent, I0, I9, charge, dt, sval,
+                                                  sflag);
   if (x < xe) {
     voltage[x] = uv_one(v, q, c, l);
     charge[x] = 0.0f;
