@@ -55,101 +55,108 @@ struct WireStep<CKT_MODE_EXACT> {
 
 // FAST: the three divisors are loop-invariant, so their quotients are
 // computed once per wire (correctly rounded) and every inner-loop divide
-// becomes a multiply; the subtract-then-scale pairs become FMAs:
-//   i_k  <- ((v_k+1 - v_k) + (-L/dt) * (i_k - I0_k)) * (1/R)
-//   v_k+1 <- (dt/C) * (i_k - i_k+1) + V0_k
-// 4 FP32 operations per current and 2 per voltage (58 per wire-step).
-// Kept as the scalar variant of the packed step below.
+// becomes a multiply.  The step works on j_k = i_k * R, the current before
+// its 1/R scale, and carries d_k = i_k - I0_k from step to step:
+//   j_k   <- (v_k+1 - v_k) + (-L/dt) * d_k
+//   v_k+1 <- ((dt/C)(1/R)) * (j_k - j_k+1) + V0_k
+//   d_k   <- (1/R) j_k - I0_k           (every step but the last)
+//   i_k   <- (1/R) j_k                  (after the last step)
+// starting from d_k = I0_k - I0_k.  3 FP32 operations per current and 2
+// per voltage: 48 per wire-step, against the reference expression's 96
+// counted flops.  Within 1e-5 relative of EXACT in the finite regime, with
+// EXACT's NaN/Inf classes at the configured steps.
 constexpr int kModeFastScalar = CKT_MODE_FAST_SCALAR;
 
 struct FastConsts {
-  float nLdt, rR, dtC;
+  float nLdt, rR, dtC, dtCrR;
   __device__ __forceinline__ FastConsts(float l, float r, float c, float d) {
     nLdt = -__fdiv_rn(l, d);
     rR = __fdiv_rn(1.0f, r);
     dtC = __fdiv_rn(d, c);
+    dtCrR = __fmul_rn(dtC, rR);
   }
 };
 
-template <>
-struct WireStep<kModeFastScalar> {
+// Scalar form of the paired steppers below (bit-identical to them).
+// LAST: write the currents i_k into di instead of the next d_k.
+struct FastStep {
   FastConsts k;
-  __device__ __forceinline__ WireStep(float l, float r, float c, float d) : k(l, r, c, d) {}
-  __device__ __forceinline__ void step(float (&ni)[10], float (&nv)[11], const float (&I0)[10],
+  __device__ __forceinline__ FastStep(float l, float r, float c, float d) : k(l, r, c, d) {}
+  template <bool LAST>
+  __device__ __forceinline__ void step(float (&di)[10], float (&nv)[11], const float (&I0)[10],
                                        const float (&V0)[9]) const {
+    float j[10];
 #pragma unroll
-    for (int j = 0; j < 10; j++) {
-      const float dv = __fsub_rn(nv[j + 1], nv[j]);
-      ni[j] = __fmul_rn(__fmaf_rn(k.nLdt, __fsub_rn(ni[j], I0[j]), dv), k.rR);
-    }
+    for (int q = 0; q < 10; q++) j[q] = __fmaf_rn(k.nLdt, di[q], __fsub_rn(nv[q + 1], nv[q]));
 #pragma unroll
-    for (int j = 0; j < 9; j++) nv[j + 1] = __fmaf_rn(k.dtC, __fsub_rn(ni[j], ni[j + 1]), V0[j]);
+    for (int q = 0; q < 9; q++) nv[q + 1] = __fmaf_rn(k.dtCrR, __fsub_rn(j[q], j[q + 1]), V0[q]);
+#pragma unroll
+    for (int q = 0; q < 10; q++) di[q] = LAST ? __fmul_rn(k.rR, j[q]) : __fmaf_rn(k.rR, j[q], -I0[q]);
   }
 };
 
 // FAST, packed: the same operations, two at a time with Blackwell's paired
 // FP32 instructions (add/mul/fma .f32x2).  Segment k is paired with k+5:
-// currents (i_p, i_p+5) for p < 5 and voltages (v_q, v_q+5) for q <= 5, so
+// currents (d_p, d_p+5) for p < 5 and voltages (v_q, v_q+5) for q <= 5, so
 // every current operation and all voltages but v5 are one paired
 // instruction for two segments.  A difference a - b is fma(b, -1, a):
 // exact product, one rounding -- the same bits as the subtraction.  Each
-// component is rounded exactly as in the scalar step, so the results are
-// bit-identical to it; the instruction count drops from 58 to 31 per
-// wire-step.
+// component is rounded exactly as in the scalar step: bit-identical to it.
 struct PackedFast {
-  float2 nLdt, rR, dtC, neg1;
-  float dtC1;
+  float2 nLdt, rR, dtCrR, neg1;
+  float dtCrR1;
   __device__ __forceinline__ PackedFast(float l, float r, float c, float d) {
     const FastConsts k(l, r, c, d);
     nLdt = make_float2(k.nLdt, k.nLdt);
     rR = make_float2(k.rR, k.rR);
-    dtC = make_float2(k.dtC, k.dtC);
+    dtCrR = make_float2(k.dtCrR, k.dtCrR);
     neg1 = make_float2(-1.0f, -1.0f);
-    dtC1 = k.dtC;
+    dtCrR1 = k.dtCrR;
   }
-  // ip[p] = (i_p, i_p+5); nI0[p] = (-I0_p, -I0_p+5); vp[q] = (v_q, v_q+5);
+  // dp[p] = (d_p, d_p+5); nI0[p] = (-I0_p, -I0_p+5); vp[q] = (v_q, v_q+5);
   // V0p[j] = (V0_j, V0_j+5) for j < 4; V04 = V0_4.
-  __device__ __forceinline__ void step(float2 (&ip)[5], float2 (&vp)[6], const float2 (&nI0)[5],
+  template <bool LAST>
+  __device__ __forceinline__ void step(float2 (&dp)[5], float2 (&vp)[6], const float2 (&nI0)[5],
                                        const float2 (&V0p)[4], float V04) const {
+    float2 jp[5];
 #pragma unroll
-    for (int p = 0; p < 5; p++) {
-      const float2 dv = __ffma2_rn(vp[p], neg1, vp[p + 1]);
-      const float2 di = __fadd2_rn(ip[p], nI0[p]);
-      ip[p] = __fmul2_rn(__ffma2_rn(nLdt, di, dv), rR);
-    }
+    for (int p = 0; p < 5; p++) jp[p] = __ffma2_rn(nLdt, dp[p], __ffma2_rn(vp[p], neg1, vp[p + 1]));
 #pragma unroll
     for (int q = 1; q < 5; q++)
-      vp[q] = __ffma2_rn(dtC, __ffma2_rn(ip[q], neg1, ip[q - 1]), V0p[q - 1]);
-    const float v5 = __fmaf_rn(dtC1, __fmaf_rn(ip[0].y, -1.0f, ip[4].x), V04);
+      vp[q] = __ffma2_rn(dtCrR, __ffma2_rn(jp[q], neg1, jp[q - 1]), V0p[q - 1]);
+    const float v5 = __fmaf_rn(dtCrR1, __fmaf_rn(jp[0].y, -1.0f, jp[4].x), V04);
     vp[0].y = v5;
     vp[5].x = v5;
+#pragma unroll
+    for (int p = 0; p < 5; p++) dp[p] = LAST ? __fmul2_rn(rR, jp[p]) : __ffma2_rn(rR, jp[p], nI0[p]);
   }
 };
 
 // FAST, two wires per thread: wire a's segment k and wire b's segment k
-// share every paired instruction, so all 58 operations of a wire-step pair
-// up with no cross-lane moves (29 instructions per wire-step).  Each lane is
+// share every paired instruction, so all 48 operations of a wire-step pair
+// up with no cross-lane moves (24 instructions per wire-step).  Each lane is
 // rounded exactly as the scalar step: bit-identical to it.
 struct DualFast {
-  float2 nLdt, rR, dtC, neg1;
+  float2 nLdt, rR, dtCrR, neg1;
   __device__ __forceinline__ DualFast(float2 l, float2 r, float2 c, float d) {
     const FastConsts ka(l.x, r.x, c.x, d), kb(l.y, r.y, c.y, d);
     nLdt = make_float2(ka.nLdt, kb.nLdt);
     rR = make_float2(ka.rR, kb.rR);
-    dtC = make_float2(ka.dtC, kb.dtC);
+    dtCrR = make_float2(ka.dtCrR, kb.dtCrR);
     neg1 = make_float2(-1.0f, -1.0f);
   }
-  // ni[k] = (i_k of a, i_k of b), nv[k] likewise; nI0 = -I0; V0 = wire voltages.
-  __device__ __forceinline__ void step(float2 (&ni)[10], float2 (&nv)[11], const float2 (&nI0)[10],
+  // d[k] = (d_k of a, d_k of b), nv[k] likewise; nI0 = -I0; V0 = wire voltages.
+  template <bool LAST>
+  __device__ __forceinline__ void step(float2 (&d)[10], float2 (&nv)[11], const float2 (&nI0)[10],
                                        const float2 (&V0)[9]) const {
+    float2 j[10];
 #pragma unroll
-    for (int k = 0; k < 10; k++) {
-      const float2 dv = __ffma2_rn(nv[k], neg1, nv[k + 1]);
-      const float2 di = __fadd2_rn(ni[k], nI0[k]);
-      ni[k] = __fmul2_rn(__ffma2_rn(nLdt, di, dv), rR);
-    }
+    for (int k = 0; k < 10; k++) j[k] = __ffma2_rn(nLdt, d[k], __ffma2_rn(nv[k], neg1, nv[k + 1]));
 #pragma unroll
-    for (int k = 0; k < 9; k++) nv[k + 1] = __ffma2_rn(dtC, __ffma2_rn(ni[k + 1], neg1, ni[k]), V0[k]);
+    for (int k = 0; k < 9; k++)
+      nv[k + 1] = __ffma2_rn(dtCrR, __ffma2_rn(j[k + 1], neg1, j[k]), V0[k]);
+#pragma unroll
+    for (int k = 0; k < 10; k++) d[k] = LAST ? __fmul2_rn(rR, j[k]) : __ffma2_rn(rR, j[k], nI0[k]);
   }
 };
 
@@ -201,35 +208,55 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
 
   if constexpr (MODE == CKT_MODE_FAST) {
     const PackedFast pk(a.L[w], a.R[w], a.C[w], dt);
-    float2 ip[5], nI0[5], vp[6], V0p[4];
+    float2 dp[5], nI0[5], vp[6], V0p[4];
 #pragma unroll
     for (int p = 0; p < 5; p++) {
-      ip[p] = make_float2(ni[p], ni[p + 5]);
       nI0[p] = make_float2(-I0[p], -I0[p + 5]);
+      dp[p] = __fadd2_rn(make_float2(I0[p], I0[p + 5]), nI0[p]);
     }
 #pragma unroll
     for (int q = 0; q < 6; q++) vp[q] = make_float2(nv[q], nv[q + 5]);
 #pragma unroll
     for (int q = 0; q < 4; q++) V0p[q] = make_float2(V0[q], V0[q + 5]);
-    int j = 0;
+    if (steps > 0) {
+      int j = 1;
 #pragma unroll 1
-    for (; j + 4 <= steps; j += 4) {
-      pk.step(ip, vp, nI0, V0p, V0[4]);
-      pk.step(ip, vp, nI0, V0p, V0[4]);
-      pk.step(ip, vp, nI0, V0p, V0[4]);
-      pk.step(ip, vp, nI0, V0p, V0[4]);
-    }
+      for (; j + 4 <= steps; j += 4) {
+        pk.step<false>(dp, vp, nI0, V0p, V0[4]);
+        pk.step<false>(dp, vp, nI0, V0p, V0[4]);
+        pk.step<false>(dp, vp, nI0, V0p, V0[4]);
+        pk.step<false>(dp, vp, nI0, V0p, V0[4]);
+      }
 #pragma unroll 1
-    for (; j < steps; j++) pk.step(ip, vp, nI0, V0p, V0[4]);
+      for (; j < steps; j++) pk.step<false>(dp, vp, nI0, V0p, V0[4]);
+      pk.step<true>(dp, vp, nI0, V0p, V0[4]);
 #pragma unroll
-    for (int p = 0; p < 5; p++) {
-      ni[p] = ip[p].x;
-      ni[p + 5] = ip[p].y;
+      for (int p = 0; p < 5; p++) {
+        ni[p] = dp[p].x;
+        ni[p + 5] = dp[p].y;
+      }
+#pragma unroll
+      for (int q = 0; q < 6; q++) {
+        nv[q] = vp[q].x;
+        nv[q + 5] = vp[q].y;
+      }
     }
+  } else if constexpr (MODE == kModeFastScalar) {
+    const FastStep fs(a.L[w], a.R[w], a.C[w], dt);
+    if (steps > 0) {
+      float d[10];
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
-      nv[q] = vp[q].x;
-      nv[q + 5] = vp[q].y;
+      for (int k = 0; k < 10; k++) d[k] = __fsub_rn(I0[k], I0[k]);
+      int j = 1;
+#pragma unroll 1
+      for (; j + 2 <= steps; j += 2) {
+        fs.step<false>(d, nv, I0, V0);
+        fs.step<false>(d, nv, I0, V0);
+      }
+      if (j < steps) fs.step<false>(d, nv, I0, V0);
+      fs.step<true>(d, nv, I0, V0);
+#pragma unroll
+      for (int k = 0; k < 10; k++) ni[k] = d[k];
     }
   } else {
     const WireStep<MODE> ws(a.L[w], a.R[w], a.C[w], dt);
@@ -259,12 +286,12 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
                                               const WireArrays &a, const NodeVolts &nvin,
                                               int steps, float dt) {
   const int64_t S = a.S;
-  float2 ni[10], nI0[10], nv[11], V0[9];
+  float2 ni[10], nI0[10], nv[11], V0[9];  // ni: d_k during the loop, then the currents
 #pragma unroll
   for (int k = 0; k < 10; k++) {
     const float x = a.cur[k * S + wa], y = a.cur[k * S + wb];
-    ni[k] = make_float2(x, y);
     nI0[k] = make_float2(-x, -y);
+    ni[k] = __fadd2_rn(make_float2(x, y), nI0[k]);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) V0[k] = make_float2(a.vol[k * S + wa], a.vol[k * S + wb]);
@@ -283,13 +310,19 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
   nv[10] = make_float2(out_a, out_b);
   const DualFast pk(make_float2(a.L[wa], a.L[wb]), make_float2(a.R[wa], a.R[wb]),
                     make_float2(a.C[wa], a.C[wb]), dt);
-  int j = 0;
+  if (steps > 0) {
+    int j = 1;
 #pragma unroll 1
-  for (; j + 2 <= steps; j += 2) {
-    pk.step(ni, nv, nI0, V0);
-    pk.step(ni, nv, nI0, V0);
+    for (; j + 2 <= steps; j += 2) {
+      pk.step<false>(ni, nv, nI0, V0);
+      pk.step<false>(ni, nv, nI0, V0);
+    }
+    if (j < steps) pk.step<false>(ni, nv, nI0, V0);
+    pk.step<true>(ni, nv, nI0, V0);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 10; k++) ni[k] = make_float2(-nI0[k].x, -nI0[k].y);  // no step: I0
   }
-  if (j < steps) pk.step(ni, nv, nI0, V0);
 #pragma unroll
   for (int k = 0; k < 10; k++) a.cur[k * S + wa] = ni[k].x;
 #pragma unroll
@@ -305,7 +338,7 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
 constexpr int kPairBlock = 256;  // threads; a block covers 2 * kPairBlock wires
 
 template <int INIT>
-__global__ void __launch_bounds__(kPairBlock)
+__global__ void __launch_bounds__(kPairBlock, 2)
     cnc_pair_kernel(uint32_t first_wire, uint32_t num_wires, WireArrays a, NodeVolts v, int steps,
                     float dt) {
   const uint32_t ta = blockIdx.x * (2 * kPairBlock) + threadIdx.x, tb = ta + kPairBlock;
