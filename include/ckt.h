@@ -54,11 +54,14 @@ typedef enum {
    * divides, no contraction): bit-identical to the reference CPU task. */
   CKT_MODE_EXACT = 0,
   /* Loop-invariant quotients L/dt, 1/R and dt/C hoisted out of the inner
-   * loop and fused multiply-adds: within 1e-5 relative of EXACT.  Issued as
-   * paired FP32 instructions (two segments per instruction). */
+   * loop, each current carried before its 1/R scale, fused multiply-adds:
+   * 48 FP32 operations per wire-step, within 1e-5 relative of EXACT in the
+   * finite regime and with its NaN/Inf classes.  Issued as paired FP32
+   * instructions (two wires per instruction in the per-piece and
+   * index-space kernels, two segments in the batched kernel). */
   CKT_MODE_FAST = 1,
-  /* FAST arithmetic issued one segment per instruction: bit-identical to
-   * CKT_MODE_FAST (kept to check the paired form and to measure it). */
+  /* FAST arithmetic issued one operation per instruction: bit-identical to
+   * CKT_MODE_FAST (kept to check the paired forms and to measure them). */
   CKT_MODE_FAST_SCALAR = 2
 } ckt_mode;
 
