@@ -284,7 +284,8 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
 template <int INIT>
 __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b,
                                               const WireArrays &a, const NodeVolts &nvin,
-                                              int steps, float dt) {
+                                              int steps, float dt, float2 *i0_out = nullptr,
+                                              float2 *i9_out = nullptr) {
   const int64_t S = a.S;
   float2 ni[10], nI0[10], nv[11], V0[9];  // ni: d_k during the loop, then the currents
 #pragma unroll
@@ -333,6 +334,8 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
 #pragma unroll
     for (int k = 0; k < 9; k++) a.vol[k * S + wb] = nv[k + 1].y;
   }
+  if (i0_out) *i0_out = ni[0];
+  if (i9_out) *i9_out = ni[9];
 }
 
 constexpr int kPairBlock = 256;  // threads; a block covers 2 * kPairBlock wires
