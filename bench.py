@@ -20,7 +20,8 @@ larger than L2.
          launches), on one stream
   e2e    through ckt_run_loops_all with host buffers: every step copies the
          circuit from pinned host memory to the device, runs the 10 loops and
-         copies the resulting state back
+         copies the resulting state back; with two device copies of the
+         circuit, a step's copies overlap its neighbours' loops
   index_space_tasks  the same steps through the three separate index-space
          task launches per loop (the drop-in boundary), with their kernels
 
@@ -59,6 +60,7 @@ SHAPE = dict(num_pieces=64, nodes_per_piece=16384, wires_per_piece=65536)
 PCT, SEED, INNER_STEPS, OUTER_LOOPS = 95.0, 12345, 1000, 10
 L_OFFSET, L_SCALE = 0.001, 0.01
 FLOPS_PER_WIRE_STEP = 96  # the reference's own count (apps/circuit/circuit.cc:324)
+CNC_TRAFFIC_PER_WIRE = (103.879424e6 + 21.284608e6) / 1048576  # measured DRAM bytes per wire
 
 
 def workload_config(mode: str, pieces: int = SHAPE["num_pieces"]) -> dict:
@@ -432,7 +434,11 @@ def main() -> None:
                        f"{probe['paired'] / 1e12:.1f} TFLOP/s)",
         "algorithmic": f"{FLOPS_PER_WIRE_STEP} flops per wire-step x {shape.W} wires x "
                        f"{INNER_STEPS} steps per launch",
-        "traffic": None,
+        # ncu dram__bytes_read.sum + dram__bytes_write.sum of one FAST launch
+        # over 1,048,576 wires (103.9 + 21.3 MB), scaled by the wires: the
+        # traffic is per wire (96 B read, up to 76 B written)
+        "traffic": CNC_TRAFFIC_PER_WIRE * shape.W if mode == G.MODE_FAST else None,
+        "traffic_unit": "bytes per launch",
     }
     cnc_task_s = statistics.mean(kt_tasks["cnc"])
     kernels = {
@@ -464,24 +470,48 @@ def main() -> None:
     h2d = sum(v.numel() * v.element_size() for v in pinned.values())
     d2h = sum(v.numel() * v.element_size() for v in out_pinned.values())
 
-    def e2e_step():
-        with torch.cuda.stream(stream):
-            for k in h2d_keys:
-                dc.t[k].copy_(pinned[k], non_blocking=True)
-        G.check(L.ckt_run_loops_all(g, w, n, ctypes.byref(prm), OUTER_LOOPS, sp))
-        with torch.cuda.stream(stream):
-            for k in C.STATE_FIELDS:
-                out_pinned[k].copy_(dc.t[k], non_blocking=True)
+    # Two device copies of the circuit, so that one step's upload and the
+    # previous step's download overlap a step's loops: uploads on one copy
+    # stream, downloads on another (the two directions use separate copy
+    # engines), the loops on the compute stream.  Every step still copies
+    # its whole circuit in and its state out.
+    dc2 = C.DeviceCircuit(host, shape, device=f"cuda:{local}")
+    bufs = [(dc, g, w, n), (dc2, dc2.graph.handle, dc2.wires(), dc2.nodes())]
+    outs = [out_pinned, {k: torch.empty_like(v).pin_memory() for k, v in out_pinned.items()}]
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    freed = [None, None]  # event: buffer's last download done
 
-    for _ in range(args.warmup):
-        e2e_step()
+    def e2e_step(i):
+        b, gb, wb, nb = bufs[i % 2]
+        with torch.cuda.stream(up):
+            if freed[i % 2] is not None:
+                up.wait_event(freed[i % 2])
+            for k in h2d_keys:
+                b.t[k].copy_(pinned[k], non_blocking=True)
+            loaded = torch.cuda.Event()
+            loaded.record(up)
+        stream.wait_event(loaded)
+        G.check(L.ckt_run_loops_all(gb, wb, nb, ctypes.byref(prm), OUTER_LOOPS, sp))
+        done = torch.cuda.Event()
+        done.record(stream)
+        with torch.cuda.stream(down):
+            down.wait_event(done)
+            for k in C.STATE_FIELDS:
+                outs[i % 2][k].copy_(b.t[k], non_blocking=True)
+            freed[i % 2] = torch.cuda.Event()
+            freed[i % 2].record(down)
+
+    for i in range(args.warmup):
+        e2e_step(i)
     torch.cuda.synchronize()
     barrier()
     e0, e1 = E(), E()
     w0 = time.perf_counter()
     e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    up.wait_event(e0)
+    for i in range(args.steps):
+        e2e_step(args.warmup + i)
+    stream.wait_stream(down)
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
@@ -489,7 +519,10 @@ def main() -> None:
     e2e_total, e2e_s, _ = replicas.aggregate(updates_per_step * args.steps,
                                              max(e0.elapsed_time(e1) * 1e-3, wall), device="cuda")
     e2e = {"value": e2e_total / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "note": "ckt_run_loops_all on host buffers: every step uploads the whole circuit from "
+                   "pinned memory and downloads its state; two device copies let one step's "
+                   "copies overlap the neighbouring step's loops"}
 
     if rank == 0:
         line = {
