@@ -478,11 +478,9 @@ int ckt_batch_run_sequential(ckt_batch *b, int32_t mode, int32_t per_piece, void
     } else if ((rc = launch_cnc(0, c.W, w, c.nvolt, c.nvolt, c.nvolt, &prm, s))) {
       return rc;
     }
-    if (c.W > 0) {
-      dc_scatter_kernel<<<grid_for(c.W), 256, 0, s>>>(c.W, c.slot_in, c.slot_out, c.cur,
-                                                      c.cur + 9 * (size_t)c.W, c.contrib, prm.dt);
-      CKT_CHECK_LAUNCH();
-      dc_sum_kernel<<<grid_for(c.N), 256, 0, s>>>(0u, c.N, c.off, c.contrib, c.gstart, c.charge);
+    if (c.W > 0 && c.N > 0) {  // the plain path's distribute_charge
+      dc_all_kernel<<<grid_for(c.N, kDcBlock), kDcBlock, 0, s>>>(
+          0u, c.N, c.off, c.ent, c.cur, c.cur + 9 * (size_t)c.W, c.charge, prm.dt);
       CKT_CHECK_LAUNCH();
     }
     if (per_piece) {

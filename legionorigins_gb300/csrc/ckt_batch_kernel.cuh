@@ -125,7 +125,7 @@ __device__ __forceinline__ void uv_tile(const RoundCircuit &rc, uint32_t x0, uin
 }
 
 // DC over local nodes [x0, xe) from the contribution buffer the CNC tiles
-// filled (DC schedule 2).  Same order as dc_sum_kernel.
+// filled (DC schedule 2).  Same order as dc_block.
 template <uint32_t BLOCK>
 __device__ __forceinline__ void dc_contrib_block(const RoundCircuit &rc, uint32_t x0, uint32_t xe,
                                                  float *sval) {
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(BLOCK, (MODE == CKT_MODE_FAST && WPT == 2 ? 51
                  uint64_t timeout_ns) {
   __shared__ uint32_t s_item, s_go;
   __shared__ float sval[DCS == 1 ? 1 : kDcChunk];
-  __shared__ uint8_t sflag[DCS == 0 ? kDcChunk : 1];
+  __shared__ uint32_t smask[DCS == 0 ? kDcChunk / 32 : 1];
   while (true) {
     if (threadIdx.x == 0) {
       const uint32_t it = atomicAdd(sync.ticket, 1u);
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(BLOCK, (MODE == CKT_MODE_FAST && WPT == 2 ? 51
     } else if (kind == kItemDc) {
       if (DCS == 0) {
         dc_block<BLOCK, true>(item.begin, item.begin + item.count, rc.off, rc.ent, rc.cur,
-                              rc.cur + 9 * (size_t)rc.W, rc.charge, dt, sval, sflag);
+                              rc.cur + 9 * (size_t)rc.W, rc.charge, dt, sval, smask);
       } else if (DCS == 1) {
         if (threadIdx.x < item.count)
           dc_node<true>(item.begin + threadIdx.x, rc.off, rc.ent, rc.cur,

@@ -399,7 +399,7 @@ __device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
                                          const float *__restrict__ I0,
                                          const float *__restrict__ I9,
                                          float *__restrict__ charge, float dt, float *sval,
-                                         uint8_t *sflag) {
+                                         uint32_t *smask) {
   const uint32_t x = x0 + threadIdx.x;
   const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
   uint32_t b = 0, e = 0;
@@ -434,9 +434,11 @@ __device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
 #pragma unroll
       for (uint32_t r = 0; r < kDcBatch; r++) {
         const uint32_t j = j0 + r * BLOCK + threadIdx.x;
+        // group-start flags of the warp's 32 consecutive entries, one word
+        const uint32_t m = __ballot_sync(0xffffffffu, (u[r] & 1u) != 0u);
         if (j < cn) {
           sval[j] = (u[r] & 2u) ? __fmul_rn(dt, v[r]) : __fmul_rn(-dt, v[r]);
-          sflag[j] = (uint8_t)(u[r] & 1u);
+          if ((threadIdx.x & 31u) == 0u) smask[j >> 5] = m;
         }
       }
     }
@@ -446,7 +448,7 @@ __device__ __forceinline__ float dc_block(uint32_t x0, uint32_t xe,
       for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sval[i - c0]);
     } else {
       for (uint32_t i = i0; i < i1; i++) {
-        if (sflag[i - c0] && i != b) {
+        if (((smask[(i - c0) >> 5] >> ((i - c0) & 31u)) & 1u) && i != b) {
           acc = __fadd_rn(acc, fold);
           fold = 0.0f;
         }
@@ -495,67 +497,6 @@ __device__ __forceinline__ void dc_node(uint32_t x, const uint32_t *__restrict__
   charge[x] = acc;
 }
 
-// Two-pass form (whole circuit).  Pass 1, one thread per wire: read I[0],
-// I[9] and the CSR slots of the wire's two ends (all coalesced) and write
-// each contribution into its slot of a contribution buffer laid out like
-// the CSR.  Pass 2, a block per 256 nodes: the block's contributions are a
-// contiguous span of that buffer; stage it with coalesced loads and let
-// each thread sum its node's run in the reference order.  The piece-group
-// starts the shared nodes need come from a bit per CSR entry.
-static __global__ void __launch_bounds__(256)
-    dc_scatter_kernel(uint32_t W, const uint32_t *__restrict__ slot_in,
-                      const uint32_t *__restrict__ slot_out, const float *__restrict__ I0,
-                      const float *__restrict__ I9, float *__restrict__ contrib, float dt) {
-  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= W) return;
-  contrib[slot_in[w]] = __fmul_rn(-dt, I0[w]);
-  contrib[slot_out[w]] = __fmul_rn(dt, I9[w]);
-}
-
-static __global__ void __launch_bounds__(256)
-    dc_sum_kernel(uint32_t node_begin, uint32_t node_end, const uint32_t *__restrict__ off,
-                  const float *__restrict__ contrib, const uint32_t *__restrict__ gstart,
-                  float *__restrict__ charge) {
-  __shared__ float sval[kDcChunk];
-  const uint32_t x0 = node_begin + blockIdx.x * 256u;
-  const uint32_t xe = min(node_end, x0 + 256u);
-  const uint32_t x = x0 + threadIdx.x;
-  const uint32_t lo = off[x0] & 0x7fffffffu, hi = off[xe] & 0x7fffffffu;
-  uint32_t b = 0, e = 0;
-  bool priv = true;
-  float acc = 0.0f, fold = 0.0f;
-  if (x < xe) {
-    const uint32_t o0 = off[x], o1 = off[x + 1];
-    priv = (o0 & 0x80000000u) != 0;
-    b = o0 & 0x7fffffffu;
-    e = o1 & 0x7fffffffu;
-    acc = charge[x];
-  }
-  for (uint32_t c0 = lo; c0 < hi; c0 += kDcChunk) {
-    const uint32_t cn = min(kDcChunk, hi - c0);
-#pragma unroll 4
-    for (uint32_t j = threadIdx.x; j < cn; j += 256u) sval[j] = contrib[c0 + j];
-    __syncthreads();
-    const uint32_t i0 = max(b, c0), i1 = min(e, c0 + cn);
-    if (priv) {
-      for (uint32_t i = i0; i < i1; i++) acc = __fadd_rn(acc, sval[i - c0]);
-    } else {
-      for (uint32_t i = i0; i < i1; i++) {
-        if (i != b && ((gstart[i >> 5] >> (i & 31u)) & 1u)) {
-          acc = __fadd_rn(acc, fold);
-          fold = 0.0f;
-        }
-        fold = __fadd_rn(fold, sval[i - c0]);
-      }
-    }
-    __syncthreads();
-  }
-  if (x < xe) {
-    if (!priv && e > b) acc = __fadd_rn(acc, fold);
-    charge[x] = acc;
-  }
-}
-
 constexpr uint32_t kDcBlock = 256;
 
 static __global__ void __launch_bounds__(kDcBlock)
@@ -563,10 +504,10 @@ static __global__ void __launch_bounds__(kDcBlock)
                   const uint32_t *__restrict__ ent, const float *__restrict__ I0,
                   const float *__restrict__ I9, float *__restrict__ charge, float dt) {
   __shared__ float sval[kDcChunk];
-  __shared__ uint8_t sflag[kDcChunk];
+  __shared__ uint32_t smask[kDcChunk / 32];
   const uint32_t x0 = node_begin + blockIdx.x * kDcBlock;
   dc_block<kDcBlock, false>(x0, min(node_end, x0 + kDcBlock), off, ent, I0, I9, charge, dt, sval,
-                            sflag);
+                            smask);
 }
 
 // One piece: one thread per node the piece touches; private nodes are
@@ -663,7 +604,7 @@ static __global__ void __launch_bounds__(kDcBlock)
                 float *__restrict__ charge, float *__restrict__ voltage,
                 const float *__restrict__ cap, const float *__restrict__ leak, float dt) {
   __shared__ float sval[kDcChunk];
-  __shared__ uint8_t sflag[kDcChunk];
+  __shared__ uint32_t smask[kDcChunk / 32];
   const uint32_t x0 = blockIdx.x * kDcBlock;
   const uint32_t xe = min(N, x0 + kDcBlock);
   const uint32_t x = x0 + threadIdx.x;
@@ -674,7 +615,7 @@ static __global__ void __launch_bounds__(kDcBlock)
     l = leak[x];
   }
   const float q = dc_block<kDcBlock, false, false>(x0, xe, off, ent, I0, I9, charge, dt, sval,
-                                                  sflag);
+                                                  smask);
   if (x < xe) {
     voltage[x] = uv_one(v, q, c, l);
     charge[x] = 0.0f;

@@ -208,8 +208,8 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
   // The staged gather: measured faster than scattering the contributions
-  // into CSR order and summing them (dc_scatter_kernel + dc_sum_kernel),
-  // whose random 4-byte writes cost as much as the gathers they replace.
+  // into CSR order and summing them contiguously, whose random 4-byte writes
+  // cost as much as the gathers they replace.
   const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
   dc_all_kernel<<<grid_for(graph->N, kDcBlock), kDcBlock, 0, as_stream(stream)>>>(
       0u, (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, prm->dt);
