@@ -260,11 +260,13 @@ def main() -> None:
     ap.add_argument("--cpu-sample-s", type=float, default=3.0,
                     help="target seconds of CPU work per sampled step of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["plain", "batched", "serve", "reductions"],
+    ap.add_argument("--workload", choices=["plain", "batched", "serve", "reductions",
+                                           "generate", "layout"],
                     default="plain",
                     help="plain: 64x16384x65536 circuit (default); batched: 256 mixed circuits; "
                          "serve: Poisson request stream; reductions: the reduction "
-                         "microbenchmark (reducetest) under each schedule")
+                         "microbenchmark (reducetest) under each schedule; generate: building "
+                         "the config-1 circuit on the GPU vs the host; layout: AoS <-> SoA")
     ap.add_argument("--rates", default="100,200,400,600,800",
                     help="serve: offered request rates (requests/s) to sweep")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
@@ -305,6 +307,12 @@ def main() -> None:
         return
     if args.workload == "reductions":
         run_reductions(args, torch, G, ws, rank, local, dist)
+        return
+    if args.workload == "generate":
+        run_generate(args, torch, G, ws, rank, local, dist)
+        return
+    if args.workload == "layout":
+        run_layout(args, torch, G, ws, rank, local, dist)
         return
 
     # CPU baseline first (rank 0, N=1 only), before any GPU work is queued.
@@ -858,6 +866,130 @@ def red_cpu_baseline(args) -> dict:
     return {"value": n * bsize / secs, "unit": "reductions/s", "cores": threads, "kind": "port",
             "sample": f"{n} of {batches} batches of {bsize} ({buckets} buckets), "
                       f"oracle/ckt_oracle.c redfold on {threads} threads"}
+
+
+def run_generate(args, torch, G, ws, rank, local, dist) -> None:
+    """Building one config-1 circuit (64 x 16384 x 65536, 4,194,304 wires):
+    the reference generator and graph on the host (ckt_generate +
+    ckt_graph_create, which a host-built request pays before upload) against
+    ckt_generate_device, which leaves the same arrays and graph on the GPU."""
+    from legionorigins_gb300 import DeviceCircuitArrays, GenParams
+    from legionorigins_gb300 import circuit as C
+
+    P, npp, wpp = SHAPE["num_pieces"], SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"]
+    W, N = P * wpp, P * npp
+    t = time.perf_counter()
+    host = C.generate(P, npp, wpp, PCT, SEED, L_OFFSET, L_SCALE)
+    t_gen = time.perf_counter() - t
+    t = time.perf_counter()
+    g = C.Graph(C.Shape(P, npp, wpp).pieces(), N, host["in_ptr"], host["out_ptr"], host["in_loc"],
+                host["out_loc"])
+    t_graph = time.perf_counter() - t
+    g.close()
+    dev = {
+        "in_ptr": (W, torch.int32), "out_ptr": (W, torch.int32), "in_loc": (W, torch.uint8),
+        "out_loc": (W, torch.uint8), "inductance": (W, torch.float32),
+        "resistance": (W, torch.float32), "capacitance": (W, torch.float32),
+        "current": (10 * W, torch.float32), "voltage": (9 * W, torch.float32),
+        "charge": (N, torch.float32), "node_voltage": (N, torch.float32),
+        "node_capacitance": (N, torch.float32), "node_leakage": (N, torch.float32),
+        "locator": (N, torch.int32), "off": (N + 1, torch.int32), "ent": (2 * W, torch.int32),
+        "slot_in": (W, torch.int32), "slot_out": (W, torch.int32),
+        "gstart": ((2 * W + 31) // 32, torch.int32)}
+    d = {k: torch.empty(n, dtype=t_, device="cuda") for k, (n, t_) in dev.items()}
+    arr = DeviceCircuitArrays(*[d[k].data_ptr() for k, _ in DeviceCircuitArrays._fields_])
+    gp = GenParams(P, npp, wpp, 0, PCT, SEED, L_OFFSET, L_SCALE)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        G.check(G.lib().ckt_generate_device(ctypes.byref(gp), ctypes.byref(arr), sp))
+    torch.cuda.synchronize()
+    ts = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            G.check(G.lib().ckt_generate_device(ctypes.byref(gp), ctypes.byref(arr), sp))
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+    same = all(np.array_equal(d[k].cpu().numpy().view(host[h].dtype), host[h])
+               for k, h in (("in_ptr", "in_ptr"), ("out_ptr", "out_ptr"), ("inductance", "L")))
+    dev_s = statistics.median(ts)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "circuit build time, 4,194,304-wire config-1 circuit with its graph",
+            "value": 1e3 * dev_s, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32/f32",
+            "data": "synthetic (the reference generator, seed 12345)",
+            "config": {"workload": "ckt_generate_device: generator + node CSR on the GPU",
+                       "wires": W, "nodes": N},
+            "host_ms": {"generate": 1e3 * t_gen, "graph": 1e3 * t_graph,
+                        "threads": "library default"},
+            "speedup_over_host": (t_gen + t_graph) / dev_s, "matches_host_sample": same,
+            "gpu_launches": None, "clocks": clk.summary()}), flush=True)
+
+
+def run_layout(args, torch, G, ws, rank, local, dist) -> None:
+    """AoS <-> SoA conversion of a config-1 circuit's wires (4,194,304 x 128-byte
+    CircuitWire): from device memory, and from pinned host memory mapped for
+    the device (zero-copy over NVLink-C2C)."""
+    from legionorigins_gb300 import circuit as C
+
+    P, npp, wpp = SHAPE["num_pieces"], SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"]
+    shape = C.Shape(P, npp, wpp)
+    host = C.generate(P, npp, wpp, PCT, SEED, L_OFFSET, L_SCALE)
+    dc = C.DeviceCircuit(host, shape, device="cuda")
+    W = shape.W
+    aos_dev = torch.zeros(128 * W, dtype=torch.uint8, device="cuda")
+    aos_host = torch.zeros(128 * W, dtype=torch.uint8).pin_memory()
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    soa_bytes = 98 * W  # in/out 8, locations 2, L/R/C 12, current 40, voltage 36
+    L = G.lib()
+    cases = {
+        "to_aos_device": lambda: L.ckt_wires_to_aos(dc.wires(), W, aos_dev.data_ptr(), sp),
+        "from_aos_device": lambda: L.ckt_wires_from_aos(aos_dev.data_ptr(), W, dc.wires(), sp),
+        "to_aos_host_mapped": lambda: L.ckt_wires_to_aos(dc.wires(), W, aos_host.data_ptr(), sp),
+        "from_aos_host_mapped": lambda: L.ckt_wires_from_aos(aos_host.data_ptr(), W, dc.wires(),
+                                                             sp),
+    }
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    with Clocks(local) as clk:
+        for name, fn in cases.items():
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    G.check(fn())
+                ts = []
+                for _ in range(args.steps):
+                    flush.fill_(1)
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    G.check(fn())
+                    b.record(stream)
+                    b.synchronize()
+                    ts.append(a.elapsed_time(b) * 1e-3)
+            sec = statistics.median(ts)
+            out[name] = {"ms": 1e3 * sec, "gbs": (128 * W + soa_bytes) / sec / 1e9,
+                         "frac_hbm": (128 * W + soa_bytes) / sec / 1e9 / hbm}
+    torch.cuda.synchronize()
+    if rank == 0:
+        head = out["from_aos_device"]
+        print(json.dumps({
+            "metric": "AoS -> SoA wire conversion bandwidth, 4,194,304 CircuitWire (128 B)",
+            "value": head["gbs"], "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32/f32",
+            "data": "synthetic (the reference generator, seed 12345)",
+            "config": {"workload": "ckt_wires_from_aos / ckt_wires_to_aos on the config-1 wires",
+                       "bytes_per_call": 128 * W + soa_bytes,
+                       "l2": "flushed (256 MB write) before every timed call"},
+            "cases": out, "hbm_peak_gbs": hbm, "gpu_launches": 4 * args.steps,
+            "clocks": clk.summary()}), flush=True)
 
 
 def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
