@@ -533,6 +533,12 @@ def main() -> None:
                    "copies overlap the neighbouring step's loops"}
 
     if rank == 0:
+        # the reference app's own report (apps/circuit/circuit.cc:314-333), per
+        # simulation of OUTER_LOOPS loops, on stderr beside the JSON line
+        sim_time = elapsed / args.steps
+        ops = (shape.W * (10 * 6 + 9 * 4) * INNER_STEPS + shape.W * 4 + shape.N * 4) * OUTER_LOOPS
+        print(f"ELAPSED TIME = {sim_time:7.3f} s", file=sys.stderr)
+        print(f"GFLOPS = {1e-9 * ops / sim_time:7.3f} GFLOPS", file=sys.stderr)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,

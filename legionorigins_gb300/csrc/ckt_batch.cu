@@ -433,6 +433,7 @@ int ckt_batch_reset_state(ckt_batch *b, void *stream) {
 }
 
 int ckt_batch_run(ckt_batch *b, int32_t mode, void *stream) {
+  NvtxRange range("ckt_batch_run");
   CKT_REQUIRE(b != nullptr, "batch is NULL");
   int rc = check_mode(mode);
   if (rc || (rc = ensure_graph(b, mode))) return rc;
@@ -508,6 +509,7 @@ int ckt_batch_run_sequential(ckt_batch *b, int32_t mode, int32_t per_piece, void
 }
 
 int ckt_batch_autotune(ckt_batch *b, int32_t mode, void *stream, ckt_batch_config *chosen) {
+  NvtxRange range("ckt_batch_autotune");
   CKT_REQUIRE(b != nullptr, "batch is NULL");
   int rc = check_mode(mode);
   if (rc) return rc;

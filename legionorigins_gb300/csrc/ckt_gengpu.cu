@@ -318,6 +318,7 @@ __global__ void csr_finish_kernel(GenArgs g, uint32_t *off, const int32_t *locat
 using namespace ckt;
 
 extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *o, void *stream) {
+  NvtxRange range("ckt_generate_device");
   CKT_REQUIRE(p != nullptr && o != nullptr, "NULL argument");
   const int32_t P = p->num_pieces, npp = p->nodes_per_piece, wpp = p->wires_per_piece;
   CKT_REQUIRE(P >= 1 && npp >= 1 && wpp >= 0, "bad shape P=%d npp=%d wpp=%d", P, npp, wpp);

@@ -321,6 +321,7 @@ int ckt_hist_scratch_bytes(const ckt_hist_params *p, int32_t schedule, uint64_t 
 
 int ckt_hist_run(const ckt_hist_params *p, int32_t schedule, uint32_t *hist, void *scratch,
                  uint64_t scratch_bytes, void *stream) {
+  NvtxRange range("ckt_hist_run");
   Plan pl;
   int rc;
   if ((rc = make_plan(p, schedule, &pl))) return rc;

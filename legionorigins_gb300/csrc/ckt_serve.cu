@@ -413,6 +413,7 @@ void sched_loop(ckt_server *s) {
       }
     }
     // One round over the active set.
+    NvtxRange range("ckt_server_round");
     circ.resize(active.size());
     for (size_t k = 0; k < active.size(); k++) {
       circ[k] = active[k]->rc;

@@ -301,6 +301,7 @@ int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
 
 int ckt_run_loops_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                       const ckt_params *prm, int32_t loops, void *stream) {
+  NvtxRange range("ckt_run_loops_all");
   int rc;
   CKT_REQUIRE(graph != nullptr, "graph is NULL");
   if ((rc = validate_params(prm)) || (rc = validate_nodes(nodes, "nodes"))) return rc;

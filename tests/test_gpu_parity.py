@@ -129,6 +129,21 @@ def test_per_piece_calls_equal_index_space(cuda, oracle, shape):
         assert same_bits(a[k], getattr(c, k)), k
 
 
+@pytest.mark.parametrize("P", [1, 2, 4])
+@pytest.mark.parametrize("npp", [1, 2, 3])
+@pytest.mark.parametrize("wpp", [1, 3, 8])
+def test_small_shapes_exact(cuda, oracle, P, npp, wpp):
+    """Every small shape: one piece, one node per piece (each in-piece wire
+    has in == out), ragged wire counts; index-space and per-piece calls."""
+    c = oracle.generate(oracle.GenParams(P, npp, wpp, 50, 7 * P + npp + wpp, L_offset=0.001))
+    a = run_gpu(cuda, device(cuda, c), 2, 2, mode=0)
+    b = run_gpu(cuda, device(cuda, c), 2, 2, mode=0, per_piece=True)
+    oracle.simulate(c, 2, 2)
+    for k in STATE:
+        assert same_bits(a[k], getattr(c, k)), k
+        assert same_bits(b[k], getattr(c, k)), k
+
+
 @pytest.mark.parametrize("shape", sorted(SHAPES))
 @pytest.mark.parametrize("mode,init", [(0, 0), (1, 0), (2, 0), (0, 1)])
 def test_fused_loops_equal_index_space(cuda, oracle, shape, mode, init):
