@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(BLOCK, (MODE == CKT_MODE_FAST && WPT == 2 ? 51
           const bool has_b = tb < item.count;
           const uint32_t w = item.begin + ta, wb = item.begin + (has_b ? tb : ta);
           float2 i0, i9;
-          cnc_wire_pair<MODE, CKT_INIT_KERNEL>((int64_t)w, (int64_t)wb, has_b, wa, volts, rc.steps, dt,
+          cnc_wire_pair<CKT_INIT_KERNEL>((int64_t)w, (int64_t)wb, has_b, wa, volts, rc.steps, dt,
                                          &i0, &i9);
           if (DCS == 2) {
             rc.contrib[rc.slot_in[w]] = __fmul_rn(-dt, i0.x);

@@ -160,33 +160,6 @@ struct DualFast {
   }
 };
 
-// EXACT, two wires per thread: the reference expression with every add,
-// subtract and multiply issued as one paired instruction for both wires (each
-// lane correctly rounded, a - b as fma(b, -1, a)) and the divisions per lane:
-// bit-identical to WireStep<CKT_MODE_EXACT>.
-__device__ __forceinline__ float2 div2_rn(float2 a, float2 b) {
-  if (a.x != a.x && a.y != a.y) return make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
-  return make_float2(div_rn(a.x, b.x), div_rn(a.y, b.y));
-}
-
-struct DualExact {
-  float2 L, R, C, dt, neg1;
-  __device__ __forceinline__ DualExact(float2 l, float2 r, float2 c, float d)
-      : L(l), R(r), C(c), dt(make_float2(d, d)), neg1(make_float2(-1.0f, -1.0f)) {}
-  __device__ __forceinline__ void step(float2 (&ni)[10], float2 (&nv)[11], const float2 (&I0)[10],
-                                       const float2 (&V0)[9]) const {
-#pragma unroll
-    for (int k = 0; k < 10; k++) {
-      const float2 dv = __ffma2_rn(nv[k], neg1, nv[k + 1]);
-      const float2 q = div2_rn(__fmul2_rn(L, __ffma2_rn(I0[k], neg1, ni[k])), dt);
-      ni[k] = div2_rn(__ffma2_rn(q, neg1, dv), R);
-    }
-#pragma unroll
-    for (int k = 0; k < 9; k++)
-      nv[k + 1] = __fadd2_rn(V0[k], div2_rn(__fmul2_rn(dt, __ffma2_rn(ni[k + 1], neg1, ni[k])), C));
-  }
-};
-
 __device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *pvt,
                                                       const float *shr, const float *ghost) {
   // get_node (apps/circuit/circuit_gpu.cu:40-59) without its assert: a
@@ -304,30 +277,22 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
   if (i9_out) *i9_out = ni[9];
 }
 
-// FAST and EXACT, two wires per thread (DualFast, DualExact): thread t of a block handles
+// FAST mode, two wires per thread (DualFast): thread t of a block handles
 // wires base + t and base + t + 256, so each field's loads and stores stay
 // one contiguous line per warp.  Without a partner wire the thread runs its
 // wire in both lanes and stores one.
-template <int MODE, int INIT>
+template <int INIT>
 __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b,
                                               const WireArrays &a, const NodeVolts &nvin,
                                               int steps, float dt, float2 *i0_out = nullptr,
                                               float2 *i9_out = nullptr) {
-  static_assert(MODE == CKT_MODE_FAST || MODE == CKT_MODE_EXACT, "paired modes");
   const int64_t S = a.S;
-  // FAST: ni holds d_k during the loop, then the currents; nI0 = -I0.
-  // EXACT: ni holds the currents throughout; nI0 = +I0.
-  float2 ni[10], nI0[10], nv[11], V0[9];
+  float2 ni[10], nI0[10], nv[11], V0[9];  // ni: d_k during the loop, then the currents
 #pragma unroll
   for (int k = 0; k < 10; k++) {
     const float x = a.cur[k * S + wa], y = a.cur[k * S + wb];
-    if constexpr (MODE == CKT_MODE_FAST) {
-      nI0[k] = make_float2(-x, -y);
-      ni[k] = __fadd2_rn(make_float2(x, y), nI0[k]);
-    } else {
-      nI0[k] = make_float2(x, y);
-      ni[k] = nI0[k];
-    }
+    nI0[k] = make_float2(-x, -y);
+    ni[k] = __fadd2_rn(make_float2(x, y), nI0[k]);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) V0[k] = make_float2(a.vol[k * S + wa], a.vol[k * S + wb]);
@@ -344,32 +309,20 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
     nv[9] = make_float2(0.0f, 0.0f);
   }
   nv[10] = make_float2(out_a, out_b);
-  const float2 l2 = make_float2(a.L[wa], a.L[wb]), r2 = make_float2(a.R[wa], a.R[wb]),
-               c2 = make_float2(a.C[wa], a.C[wb]);
-  if constexpr (MODE == CKT_MODE_FAST) {
-    const DualFast pk(l2, r2, c2, dt);
-    if (steps > 0) {
-      int j = 1;
-#pragma unroll 1
-      for (; j + 2 <= steps; j += 2) {
-        pk.step<false>(ni, nv, nI0, V0);
-        pk.step<false>(ni, nv, nI0, V0);
-      }
-      if (j < steps) pk.step<false>(ni, nv, nI0, V0);
-      pk.step<true>(ni, nv, nI0, V0);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 10; k++) ni[k] = make_float2(-nI0[k].x, -nI0[k].y);  // no step: I0
-    }
-  } else {
-    const DualExact ex(l2, r2, c2, dt);
-    int j = 0;
+  const DualFast pk(make_float2(a.L[wa], a.L[wb]), make_float2(a.R[wa], a.R[wb]),
+                    make_float2(a.C[wa], a.C[wb]), dt);
+  if (steps > 0) {
+    int j = 1;
 #pragma unroll 1
     for (; j + 2 <= steps; j += 2) {
-      ex.step(ni, nv, nI0, V0);
-      ex.step(ni, nv, nI0, V0);
+      pk.step<false>(ni, nv, nI0, V0);
+      pk.step<false>(ni, nv, nI0, V0);
     }
-    if (j < steps) ex.step(ni, nv, nI0, V0);
+    if (j < steps) pk.step<false>(ni, nv, nI0, V0);
+    pk.step<true>(ni, nv, nI0, V0);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 10; k++) ni[k] = make_float2(-nI0[k].x, -nI0[k].y);  // no step: I0
   }
 #pragma unroll
   for (int k = 0; k < 10; k++) a.cur[k * S + wa] = ni[k].x;
@@ -387,15 +340,15 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
 
 constexpr int kPairBlock = 256;  // threads; a block covers 2 * kPairBlock wires
 
-template <int MODE, int INIT>
+template <int INIT>
 __global__ void __launch_bounds__(kPairBlock, 2)
     cnc_pair_kernel(uint32_t first_wire, uint32_t num_wires, WireArrays a, NodeVolts v, int steps,
                     float dt) {
   const uint32_t ta = blockIdx.x * (2 * kPairBlock) + threadIdx.x, tb = ta + kPairBlock;
   if (ta >= num_wires) return;
   const bool has_b = tb < num_wires;
-  cnc_wire_pair<MODE, INIT>((int64_t)first_wire + ta, (int64_t)first_wire + (has_b ? tb : ta),
-                            has_b, a, v, steps, dt);
+  cnc_wire_pair<INIT>((int64_t)first_wire + ta, (int64_t)first_wire + (has_b ? tb : ta), has_b,
+                      a, v, steps, dt);
 }
 
 template <int MODE, int INIT>

@@ -64,9 +64,9 @@ static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const f
                          const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
   const WireArrays a = wire_arrays(w);
   const NodeVolts v = {vp, vs, vg};
-  if constexpr (M == CKT_MODE_FAST || M == CKT_MODE_EXACT)  // two wires per thread, paired
-    cnc_pair_kernel<M, I><<<grid_for(n, 2 * kPairBlock), kPairBlock, 0, s>>>(first, n, a, v,
-                                                                             p->steps, p->dt);
+  if (M == CKT_MODE_FAST)  // two wires per thread, every operation paired
+    cnc_pair_kernel<I><<<grid_for(n, 2 * kPairBlock), kPairBlock, 0, s>>>(first, n, a, v,
+                                                                          p->steps, p->dt);
   else
     cnc_kernel<M, I><<<grid_for(n), 256, 0, s>>>(first, n, a, v, p->steps, p->dt);
 }
