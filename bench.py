@@ -271,6 +271,9 @@ def main() -> None:
                     help="serve: offered request rates (requests/s) to sweep")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
                     help="serve: seconds of arrivals per rate")
+    ap.add_argument("--serve-launch", default="",
+                    help="serve: round launch shape block,wires_per_thread,dc_schedule "
+                         "(default: the library's)")
     ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
                     help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
     args = ap.parse_args()
@@ -1021,7 +1024,9 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
     warm.close()
     clk_all = []
     for rate in rates:
-        srv = Server(mode=mode, prep_threads=cpu_threads(), hbm_budget_bytes=80 << 30)
+        launch = tuple(int(x) for x in args.serve_launch.split(",")) if args.serve_launch else None
+        srv = Server(mode=mode, prep_threads=cpu_threads(), hbm_budget_bytes=80 << 30,
+                     launch=launch)
         rng = random.Random(int(rate * 1000) + 7)
         t = 0.0
         arrivals = []
@@ -1076,7 +1081,7 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
                             "outer loops U{1..5}, 80 GB HBM admission budget, continuous "
                             "batching (one persistent launch per round)",
                 "mode": args.mode, "seconds_of_arrivals_per_rate": args.serve_seconds,
-                "rates_rps": rates,
+                "rates_rps": rates, "launch": args.serve_launch or "library default",
             },
             "latency_ms": quiet["latency_ms"], "latency_at_offered_rps": quiet["offered_rps"],
             "throughput_at_that_rate": quiet["throughput"],

@@ -326,3 +326,74 @@ def test_config2_heavy_reduction_full_size(cuda, oracle):
     for k in STATE:
         assert same_bits(got[k], getattr(c, k)), k
     assert (c.locator == 0).mean() > 0.3
+
+
+@pytest.mark.parametrize("shape", ["heavy_reduction", "cfg0", "all_cross"])
+def test_separate_region_instances(cuda, oracle, shape):
+    """The reference hands each task distinct region instances: private
+    nodes, the piece's own shared nodes, the piece's ghost nodes (absolute
+    indexing, only the instance's own nodes valid).  Here every instance holds
+    NaN outside its nodes, so a wire end read from the wrong instance, or a
+    charge applied to the wrong one, poisons the result.  The per-piece calls
+    on separate instances give the bits of the index-space launches."""
+    import ctypes
+
+    from legionorigins_gb300 import Nodes, check, lib
+    from legionorigins_gb300 import circuit as C
+
+    torch = cuda
+    P, npp, wpp, pct, seed = SHAPES[shape]
+    N = P * npp
+    c = oracle.generate(oracle.GenParams(P, npp, wpp, pct, seed, L_offset=0.001))
+    ref, sep = device(cuda, c), device(cuda, c)
+    prm = C.params(3, 0)
+    L = lib()
+    priv = c.locator == 1
+
+    def masked(vals, mask):
+        a = np.full(N, np.nan, np.float32)
+        a[mask] = vals[mask]
+        return torch.from_numpy(a).cuda()
+
+    pq, pv, pc, pl = (masked(x, priv) for x in (c.charge, c.node_voltage, c.cap, c.leak))
+    sq, sv, sc, sl = (masked(x, ~priv) for x in (c.charge, c.node_voltage, c.cap, c.leak))
+    pvt = Nodes(pq.data_ptr(), pv.data_ptr(), pc.data_ptr(), pl.data_ptr())
+    shr = Nodes(sq.data_ptr(), sv.data_ptr(), sc.data_ptr(), sl.data_ptr())
+    locator = torch.from_numpy(c.locator).cuda()
+    g, w = sep.graph.handle, sep.wires()
+    sf, gf = sep.shr_fold.data_ptr(), sep.ghost_fold.data_ptr()
+    for _ in range(2):
+        ref.loop_index_space(prm)
+        # calc_new_currents: the piece's own shared voltages and its ghost
+        # voltages as two more instances, from the shared instance's values
+        shv = sv.cpu().numpy()
+        keep = []
+        for k in range(P):
+            own = np.zeros(N, bool)
+            own[k * npp:(k + 1) * npp] = True
+            own &= ~priv
+            ws = slice(k * wpp, (k + 1) * wpp)
+            ghost = np.zeros(N, bool)
+            ghost[c.out_ptr[ws][c.out_loc[ws] == 2]] = True
+            ov, gv = masked(shv, own), masked(shv, ghost)
+            keep += [ov, gv]
+            check(L.ckt_calc_new_currents(ctypes.byref(sep.pieces[k]), w, pvt,
+                                          Nodes(0, ov.data_ptr(), 0, 0),
+                                          Nodes(0, gv.data_ptr(), 0, 0), ctypes.byref(prm), None))
+        # distribute_charge: private nodes in place, shared/ghost folds applied
+        # to the shared instance, piece by piece
+        for k in range(P):
+            check(L.ckt_distribute_charge(g, k, w, pvt, sf, gf, ctypes.byref(prm), None))
+            check(L.ckt_apply_fold(g, k, sf, gf, sq.data_ptr(), None))
+        for k in range(P):
+            check(L.ckt_update_voltages(ctypes.byref(sep.pieces[k]), pvt, shr,
+                                        locator.data_ptr(), None))
+        torch.cuda.synchronize()
+    a = ref.to_host()
+    b = sep.to_host()
+    for k in ("current", "voltage"):
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    got_v = np.where(priv, pv.cpu().numpy(), sv.cpu().numpy())
+    got_q = np.where(priv, pq.cpu().numpy(), sq.cpu().numpy())
+    assert np.array_equal(got_v.view(np.uint32), a["node_voltage"].view(np.uint32))
+    assert np.array_equal(got_q.view(np.uint32), a["charge"].view(np.uint32))
