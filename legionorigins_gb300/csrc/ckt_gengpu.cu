@@ -16,6 +16,7 @@
 // graph follow in data-parallel kernels; per-node contribution lists are
 // sorted by (wire, end) so the graph is identical to the host-built one.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "ckt_internal.h"
@@ -24,8 +25,9 @@ namespace ckt {
 namespace {
 
 constexpr uint64_t kA = 0x5DEECE66Dull, kC = 0xBull, kMask = 0xffffffffffffull;
-constexpr int kChunk = 1024;     // draws per chunk
-constexpr int kSuper = 64;       // chunks per super-chunk in the map composition
+constexpr int kChunk = 256;       // draws per chunk
+constexpr int kMapBlock = 256;    // chunks per block of the map composition
+constexpr int kTopTile = 1024;    // blocks per shared-memory tile of the top-level walk
 
 struct Jump {
   uint64_t a[48], c[48];  // state after 2^i draws: a[i]*x + c[i]
@@ -44,6 +46,26 @@ Jump make_jump() {
     a = (a * a) & kMask;
   }
   return j;
+}
+
+// The jump table never changes: it is copied to each device once.  (A
+// per-call copy from pageable memory would wait for the stream's earlier
+// work.)
+constexpr int kMaxDevices = 64;
+
+int ensure_jump_table() {
+  static std::mutex mu;
+  static bool loaded[kMaxDevices] = {};
+  int dev = 0;
+  CKT_CUDA(cudaGetDevice(&dev));
+  CKT_REQUIRE(dev >= 0 && dev < kMaxDevices, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!loaded[dev]) {
+    const Jump jump = make_jump();
+    CKT_CUDA(cudaMemcpyToSymbol(g_jump, &jump, sizeof(Jump)));
+    loaded[dev] = true;
+  }
+  return CKT_OK;
 }
 
 __device__ __forceinline__ uint64_t skip(uint64_t x, uint64_t d) {
@@ -90,7 +112,9 @@ __global__ void gen_nodes_kernel(GenArgs g, float *charge, float *nvolt, float *
 }
 
 // Per chunk and entry phase q: where the chain leaves the chunk (0..6 past
-// its end) and how many wires start inside it.
+// its end) and how many wires start inside it.  Only a wire's 5th draw (the
+// in-piece test) matters here, so the state advances for every draw and is
+// converted to a double only where some phase needs that test.
 __global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint8_t *exit_phase,
                                   uint32_t *count) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,12 +129,17 @@ __global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint
     n[q] = 0;
   }
   for (int64_t t = p0; t < p1 + 4; t++) {
-    const double u = draw(x);  // draw t
+    x = (kA * x + kC) & kMask;  // draw t
+    bool need = false;
+#pragma unroll
+    for (int q = 0; q < 7; q++) need |= (s[q] < p1 && s[q] + 4 == t);
+    if (!need) continue;
+    const bool cr = crosses(g, (double)x * 0x1p-48);
 #pragma unroll
     for (int q = 0; q < 7; q++)
       if (s[q] < p1 && s[q] + 4 == t) {
         n[q]++;
-        s[q] += 6 + (crosses(g, u) ? 1 : 0);
+        s[q] += 6 + (cr ? 1 : 0);
       }
   }
 #pragma unroll
@@ -120,66 +149,83 @@ __global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint
   }
 }
 
-// Composition of the maps of kSuper consecutive chunks.
-__global__ void super_maps_kernel(int64_t nchunks, const uint8_t *exit_phase,
-                                  const uint32_t *count, uint8_t *sexit, uint32_t *scount) {
-  const int64_t sc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t c0 = sc * kSuper;
-  if (c0 >= nchunks) return;
-  const int64_t c1 = min(nchunks, c0 + kSuper);
-  for (int q = 0; q < 7; q++) {
+// The chunk maps of kMapBlock consecutive chunks composed in shared memory:
+// for every phase q the block might be entered with, each chunk's entry
+// phase and the wires before it inside the block, and the block's own map.
+__global__ void __launch_bounds__(128)
+    map_block_kernel(int64_t nchunks, const uint8_t *__restrict__ exit_phase,
+                     const uint32_t *__restrict__ count, uint8_t *rel_phase, uint32_t *rel_base,
+                     uint8_t *bexit, uint32_t *bcount) {
+  __shared__ uint8_t se[kMapBlock * 7];
+  __shared__ uint32_t sc[kMapBlock * 7];
+  const int64_t c0 = (int64_t)blockIdx.x * kMapBlock;
+  const int n = (int)min((int64_t)kMapBlock, nchunks - c0);
+  for (int i = threadIdx.x; i < n * 7; i += blockDim.x) {
+    se[i] = exit_phase[c0 * 7 + i];
+    sc[i] = count[c0 * 7 + i];
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    const int q = threadIdx.x;
     int ph = q;
     uint32_t tot = 0;
-    for (int64_t c = c0; c < c1; c++) {
-      tot += count[c * 7 + ph];
-      ph = exit_phase[c * 7 + ph];
+    for (int k = 0; k < n; k++) {
+      rel_phase[(c0 + k) * 7 + q] = (uint8_t)ph;
+      rel_base[(c0 + k) * 7 + q] = tot;
+      tot += sc[k * 7 + ph];
+      ph = se[k * 7 + ph];
     }
-    sexit[sc * 7 + q] = (uint8_t)ph;
-    scount[sc * 7 + q] = tot;
+    bexit[blockIdx.x * 7 + q] = (uint8_t)ph;
+    bcount[blockIdx.x * 7 + q] = tot;
   }
 }
 
-// One thread: entry phase and first wire of every super-chunk.
-__global__ void super_scan_kernel(int64_t nsuper, const uint8_t *sexit, const uint32_t *scount,
-                                  uint8_t *sphase, uint64_t *sbase) {
+// The chain through the blocks from phase 0 (the first wire starts at the
+// first wire draw): every block's entry phase and first wire.  One block;
+// the maps pass through shared memory a tile at a time, so the walk's
+// dependent steps are shared-memory reads.
+__global__ void __launch_bounds__(256)
+    map_top_kernel(int64_t nblocks, const uint8_t *__restrict__ bexit,
+                   const uint32_t *__restrict__ bcount, uint8_t *bphase, uint64_t *bbase) {
+  __shared__ uint8_t se[kTopTile * 7];
+  __shared__ uint32_t sc[kTopTile * 7];
   int ph = 0;
   uint64_t tot = 0;
-  for (int64_t sc = 0; sc < nsuper; sc++) {
-    sphase[sc] = (uint8_t)ph;
-    sbase[sc] = tot;
-    tot += scount[sc * 7 + ph];
-    ph = sexit[sc * 7 + ph];
-  }
-}
-
-// Entry phase and first wire of every chunk.
-__global__ void chunk_scan_kernel(int64_t nchunks, const uint8_t *exit_phase,
-                                  const uint32_t *count, const uint8_t *sphase,
-                                  const uint64_t *sbase, uint8_t *cphase, uint64_t *cbase) {
-  const int64_t sc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t c0 = sc * kSuper;
-  if (c0 >= nchunks) return;
-  const int64_t c1 = min(nchunks, c0 + kSuper);
-  int ph = sphase[sc];
-  uint64_t tot = sbase[sc];
-  for (int64_t c = c0; c < c1; c++) {
-    cphase[c] = (uint8_t)ph;
-    cbase[c] = tot;
-    tot += count[c * 7 + ph];
-    ph = exit_phase[c * 7 + ph];
+  for (int64_t b0 = 0; b0 < nblocks; b0 += kTopTile) {
+    const int n = (int)min((int64_t)kTopTile, nblocks - b0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < n * 7; i += blockDim.x) {
+      se[i] = bexit[b0 * 7 + i];
+      sc[i] = bcount[b0 * 7 + i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < n; k++) {
+        bphase[b0 + k] = (uint8_t)ph;
+        bbase[b0 + k] = tot;
+        tot += sc[k * 7 + ph];
+        ph = se[k * 7 + ph];
+      }
+    }
   }
 }
 
 // Every chunk emits its wires (circuit.cc:1158-1186).
-__global__ void gen_wires_kernel(GenArgs g, int64_t base, int64_t nchunks, const uint8_t *cphase,
-                                 const uint64_t *cbase, uint32_t *in_ptr, uint32_t *out_ptr,
-                                 float *L, float *R, float *C, int32_t *locator) {
+__global__ void gen_wires_kernel(GenArgs g, int64_t base, int64_t nchunks,
+                                 const uint8_t *__restrict__ rel_phase,
+                                 const uint32_t *__restrict__ rel_base,
+                                 const uint8_t *__restrict__ bphase,
+                                 const uint64_t *__restrict__ bbase, uint32_t *in_ptr,
+                                 uint32_t *out_ptr, float *L, float *R, float *C,
+                                 int32_t *locator) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
-  int64_t w = (int64_t)cbase[c];
+  const int64_t b = c / kMapBlock;
+  const int qb = bphase[b];  // the block's entry phase selects the chunk's entry
+  int64_t w = (int64_t)bbase[b] + rel_base[c * 7 + qb];
   if (w >= g.W) return;
   const int64_t p0 = base + c * kChunk, p1 = p0 + kChunk;
-  int64_t s = p0 + cphase[c];
+  int64_t s = p0 + rel_phase[c * 7 + qb];
   uint64_t x = skip(g.seed_state, (uint64_t)s);
   while (s < p1 && w < g.W) {
     const double uR = draw(x), uL = draw(x), uC = draw(x), uIn = draw(x), uPct = draw(x);
@@ -333,8 +379,8 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
                          o->slot_in && o->slot_out && o->gstart),
               "wire arrays are NULL");
   const cudaStream_t s = as_stream(stream);
-  static const Jump jump = make_jump();
-  CKT_CUDA(cudaMemcpyToSymbolAsync(g_jump, &jump, sizeof(Jump), 0, cudaMemcpyHostToDevice, s));
+  int jr = ensure_jump_table();
+  if (jr) return jr;
   GenArgs g;
   g.P = P; g.npp = npp; g.wpp = wpp;
   g.pct = p->pct_wire_in_piece; g.L_off = p->L_offset; g.L_scale = p->L_scale;
@@ -355,18 +401,20 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
     return CKT_OK;
   }
 
-  // Scratch: chunk maps, scans, degree cursors, unsorted contributions.
+  // Scratch: chunk maps and their composition, degree cursors, unsorted
+  // contributions.
   const int64_t base = 3 * N;
   const int64_t nchunks = (7 * W + 8 + kChunk - 1) / kChunk;
-  const int64_t nsuper = (nchunks + kSuper - 1) / kSuper;
+  const int64_t nblocks = (nchunks + kMapBlock - 1) / kMapBlock;
   const int64_t scan_blocks = (N + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
-  const size_t sz_exit = nchunks * 7, sz_cnt = nchunks * 7 * 4, sz_sexit = nsuper * 7,
-               sz_scnt = nsuper * 7 * 4, sz_sph = nsuper, sz_sb = nsuper * 8, sz_cph = nchunks,
-               sz_cb = nchunks * 8, sz_deg = (N + 1) * 4, sz_sums = (scan_blocks + 1) * 4,
-               sz_tmp = 2 * W * 4;
+  const size_t sz_exit = nchunks * 7, sz_cnt = nchunks * 7 * 4, sz_rph = nchunks * 7,
+               sz_rb = nchunks * 7 * 4, sz_bexit = nblocks * 7, sz_bcnt = nblocks * 7 * 4,
+               sz_bph = nblocks, sz_bb = nblocks * 8, sz_deg = (N + 1) * 4,
+               sz_sums = (scan_blocks + 1) * 4, sz_tmp = 2 * W * 4;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-  const size_t total = al(sz_exit) + al(sz_cnt) + al(sz_sexit) + al(sz_scnt) + al(sz_sph) +
-                       al(sz_sb) + al(sz_cph) + al(sz_cb) + al(sz_deg) + al(sz_sums) + al(sz_tmp);
+  const size_t total = al(sz_exit) + al(sz_cnt) + al(sz_rph) + al(sz_rb) + al(sz_bexit) +
+                       al(sz_bcnt) + al(sz_bph) + al(sz_bb) + al(sz_deg) + al(sz_sums) +
+                       al(sz_tmp);
   char *scratch = nullptr;
   CKT_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), total, s));
   char *q = scratch;
@@ -377,12 +425,12 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   };
   uint8_t *exit_phase = (uint8_t *)take(sz_exit);
   uint32_t *count = (uint32_t *)take(sz_cnt);
-  uint8_t *sexit = (uint8_t *)take(sz_sexit);
-  uint32_t *scount = (uint32_t *)take(sz_scnt);
-  uint8_t *sphase = (uint8_t *)take(sz_sph);
-  uint64_t *sbase = (uint64_t *)take(sz_sb);
-  uint8_t *cphase = (uint8_t *)take(sz_cph);
-  uint64_t *cbase = (uint64_t *)take(sz_cb);
+  uint8_t *rel_phase = (uint8_t *)take(sz_rph);
+  uint32_t *rel_base = (uint32_t *)take(sz_rb);
+  uint8_t *bexit = (uint8_t *)take(sz_bexit);
+  uint32_t *bcount = (uint32_t *)take(sz_bcnt);
+  uint8_t *bphase = (uint8_t *)take(sz_bph);
+  uint64_t *bbase = (uint64_t *)take(sz_bb);
   uint32_t *deg = (uint32_t *)take(sz_deg);
   uint32_t *sums = (uint32_t *)take(sz_sums);
   uint32_t *tmp = (uint32_t *)take(sz_tmp);
@@ -394,17 +442,14 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
 
   chunk_maps_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(g, base, nchunks, exit_phase, count);
   ok(cudaGetLastError());
-  super_maps_kernel<<<grid_for(nsuper, 128), 128, 0, s>>>(nchunks, exit_phase, count, sexit,
-                                                          scount);
+  map_block_kernel<<<(unsigned)nblocks, 128, 0, s>>>(nchunks, exit_phase, count, rel_phase,
+                                                      rel_base, bexit, bcount);
   ok(cudaGetLastError());
-  super_scan_kernel<<<1, 1, 0, s>>>(nsuper, sexit, scount, sphase, sbase);
-  ok(cudaGetLastError());
-  chunk_scan_kernel<<<grid_for(nsuper, 128), 128, 0, s>>>(nchunks, exit_phase, count, sphase,
-                                                          sbase, cphase, cbase);
+  map_top_kernel<<<1, 256, 0, s>>>(nblocks, bexit, bcount, bphase, bbase);
   ok(cudaGetLastError());
   gen_wires_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(
-      g, base, nchunks, cphase, cbase, o->in_ptr, o->out_ptr, o->inductance, o->resistance,
-      o->capacitance, o->locator);
+      g, base, nchunks, rel_phase, rel_base, bphase, bbase, o->in_ptr, o->out_ptr,
+      o->inductance, o->resistance, o->capacitance, o->locator);
   ok(cudaGetLastError());
   ok(cudaMemsetAsync(deg, 0, sz_deg, s));
   gen_locs_kernel<<<grid_for(W), 256, 0, s>>>(g, o->in_ptr, o->out_ptr, o->locator, o->in_loc,
