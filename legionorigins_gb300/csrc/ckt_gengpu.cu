@@ -19,6 +19,7 @@
 #include <mutex>
 #include <vector>
 
+#include "ckt_drand.cuh"
 #include "ckt_internal.h"
 
 namespace ckt {
@@ -74,25 +75,30 @@ __device__ __forceinline__ uint64_t skip(uint64_t x, uint64_t d) {
   return x;
 }
 
-__device__ __forceinline__ double draw(uint64_t &x) {
+// Advances the generator state by one draw and returns it (the draw's value
+// is x * 2^-48; the drand helpers evaluate the expressions on x).
+__device__ __forceinline__ uint64_t next(uint64_t &x) {
   x = (kA * x + kC) & kMask;
-  return (double)x * 0x1p-48;
+  return x;
 }
 
-__device__ __forceinline__ uint32_t pick(double u, uint32_t piece, uint32_t npp) {
-  const int k = (int)(u * (double)npp);
-  return piece * npp + npp - 1 - (uint32_t)k;
+// random_element of the piece's node set (its reversed order, see
+// ckt_gen.cpp): first + npp - 1 - (int)(drand48() * npp).
+__device__ __forceinline__ uint32_t pick(uint64_t x, uint32_t piece, uint32_t npp) {
+  return piece * npp + npp - 1 - drand::trunc_mul(x, npp);
 }
 
 struct GenArgs {
   int32_t P, npp, wpp;
-  double pct, L_off, L_scale;
+  double L_off, L_scale;
+  uint64_t pct_thr;  // drand::pct_threshold(pct)
   uint64_t seed_state;
   int64_t W, N;
 };
 
-__device__ __forceinline__ bool crosses(const GenArgs &g, double u5) {
-  return g.P > 1 && !((100 * u5) < g.pct);
+// The wire leaves its piece: !(100 * drand48() < pct) with more than one piece.
+__device__ __forceinline__ bool crosses(const GenArgs &g, uint64_t x5) {
+  return g.P > 1 && !drand::pct_below(x5, g.pct_thr);
 }
 
 // Node values: draws 3x, 3x+1, 3x+2 (circuit.cc:1121-1125).
@@ -104,9 +110,9 @@ __global__ void gen_nodes_kernel(GenArgs g, float *charge, float *nvolt, float *
   const int64_t x1 = min(g.N, x0 + 16);
   for (int64_t n = x0; n < x1; n++) {
     charge[n] = 0.f;
-    nvolt[n] = __double2float_rn(__dsub_rn(__dmul_rn(2.0, draw(x)), 1.0));
-    cap[n] = __double2float_rn(__dadd_rn(draw(x), 1.0));
-    leak[n] = __double2float_rn(__dmul_rn((double)0.1f, draw(x)));
+    nvolt[n] = drand::node_voltage(next(x));
+    cap[n] = drand::node_capacitance(next(x));
+    leak[n] = __double2float_rn(__dmul_rn((double)0.1f, drand::value(next(x))));
     locator[n] = 1;
   }
 }
@@ -134,7 +140,7 @@ __global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint
 #pragma unroll
     for (int q = 0; q < 7; q++) need |= (s[q] < p1 && s[q] + 4 == t);
     if (!need) continue;
-    const bool cr = crosses(g, (double)x * 0x1p-48);
+    const bool cr = crosses(g, x);
 #pragma unroll
     for (int q = 0; q < 7; q++)
       if (s[q] < p1 && s[q] + 4 == t) {
@@ -228,19 +234,19 @@ __global__ void gen_wires_kernel(GenArgs g, int64_t base, int64_t nchunks,
   int64_t s = p0 + rel_phase[c * 7 + qb];
   uint64_t x = skip(g.seed_state, (uint64_t)s);
   while (s < p1 && w < g.W) {
-    const double uR = draw(x), uL = draw(x), uC = draw(x), uIn = draw(x), uPct = draw(x);
+    const uint64_t xR = next(x), xL = next(x), xC = next(x), xIn = next(x), xPct = next(x);
     const uint32_t n = (uint32_t)(w / g.wpp);
-    R[w] = __double2float_rn(__dadd_rn(__dmul_rn(uR, 10.0), 1.0));
-    L[w] = __double2float_rn(__dadd_rn(__dmul_rn(uL, g.L_scale), g.L_off));
-    C[w] = __double2float_rn(__dmul_rn(uC, 0.1));
-    in_ptr[w] = pick(uIn, n, (uint32_t)g.npp);
-    if (!crosses(g, uPct)) {
-      out_ptr[w] = pick(draw(x), n, (uint32_t)g.npp);
+    R[w] = drand::resistance(xR);
+    L[w] = __double2float_rn(__dadd_rn(__dmul_rn(drand::value(xL), g.L_scale), g.L_off));
+    C[w] = __double2float_rn(__dmul_rn(drand::value(xC), 0.1));
+    in_ptr[w] = pick(xIn, n, (uint32_t)g.npp);
+    if (!crosses(g, xPct)) {
+      out_ptr[w] = pick(next(x), n, (uint32_t)g.npp);
       s += 6;
     } else {
-      int nn = (int)(draw(x) * (double)(g.P - 1));
+      int nn = (int)drand::trunc_mul(next(x), (uint32_t)(g.P - 1));
       if (nn >= (int)n) nn++;
-      const uint32_t o = pick(draw(x), (uint32_t)nn, (uint32_t)g.npp);
+      const uint32_t o = pick(next(x), (uint32_t)nn, (uint32_t)g.npp);
       out_ptr[w] = o;
       locator[o] = 0;
       s += 7;
@@ -328,34 +334,73 @@ __global__ void csr_fill_kernel(int64_t W, const uint32_t *in_ptr, const uint32_
 
 // Per node: sort its contributions by (wire, end), then write the entries
 // with their piece-group flags, the wire ends' slots and the flag bits, and
-// mark private nodes in the offsets.
-__global__ void csr_finish_kernel(GenArgs g, uint32_t *off, const int32_t *locator, uint32_t *tmp,
-                                  uint32_t *ent, uint32_t *slot_in, uint32_t *slot_out,
-                                  uint32_t *gstart) {
-  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= g.N) return;
-  const uint32_t b = off[x] & 0x7fffffffu, e = off[x + 1] & 0x7fffffffu;
-  for (uint32_t i = b + 1; i < e; i++) {
-    const uint32_t v = tmp[i];
-    uint32_t j = i;
-    while (j > b && tmp[j - 1] > v) {
-      tmp[j] = tmp[j - 1];
-      j--;
+// mark private nodes in the offsets.  A warp takes 32 consecutive nodes: their
+// runs are one contiguous span, staged in shared memory (coalesced in and
+// out), sorted there a node per lane; a span larger than the stage is sorted
+// in place in tmp instead.
+constexpr uint32_t kFinishSpan = 512;  // entries per warp staged in shared memory
+
+__global__ void __launch_bounds__(256)
+    csr_finish_kernel(GenArgs g, uint32_t *off, const int32_t *locator, uint32_t *tmp,
+                      uint32_t *ent, uint32_t *slot_in, uint32_t *slot_out, uint32_t *gstart) {
+  __shared__ uint32_t sbuf[8][kFinishSpan];
+  const uint32_t lane = threadIdx.x & 31u, wp = threadIdx.x >> 5;
+  const int64_t x0 = ((int64_t)blockIdx.x * 8 + wp) * 32;
+  if (x0 >= g.N) return;
+  const int64_t xe = min(g.N, x0 + 32), x = x0 + lane;
+  const uint32_t lo = off[x0] & kOffsetMask, hi = off[xe] & kOffsetMask;
+  const uint32_t span = hi - lo;
+  const bool staged = span <= kFinishSpan;
+  uint32_t *buf = sbuf[wp];
+  if (staged)
+    for (uint32_t j = lane; j < span; j += 32) buf[j] = tmp[lo + j];
+  __syncwarp();
+  if (x < xe) {
+    const uint32_t b = off[x] & kOffsetMask, e = off[x + 1] & kOffsetMask;
+    uint32_t *run = staged ? buf : tmp;    // entry i lives at run[i - rb]
+    const uint32_t rb = staged ? lo : 0u;
+    for (uint32_t i = b + 1; i < e; i++) {
+      const uint32_t v = run[i - rb];
+      uint32_t j = i;
+      while (j > b && run[j - 1 - rb] > v) {
+        run[j - rb] = run[j - 1 - rb];
+        j--;
+      }
+      run[j - rb] = v;
     }
-    tmp[j] = v;
+    int64_t last_piece = -1;
+    for (uint32_t i = b; i < e; i++) {
+      const uint32_t v = run[i - rb], w = v >> 1, end = v & 1u;
+      const int64_t piece = w / g.wpp;
+      const uint32_t start = piece != last_piece ? 1u : 0u;
+      last_piece = piece;
+      const uint32_t val = (w << 2) | (end << 1) | start;
+      if (staged) {
+        buf[i - lo] = val;
+      } else {
+        ent[i] = val;
+        if (start) atomicOr(gstart + (i >> 5), 1u << (i & 31));
+      }
+      if (end) slot_out[w] = i;
+      else slot_in[w] = i;
+    }
+    if (locator[x]) atomicOr(off + x, kPrivateBit);
   }
-  int64_t last_piece = -1;
-  for (uint32_t i = b; i < e; i++) {
-    const uint32_t v = tmp[i], w = v >> 1, end = v & 1u;
-    const int64_t piece = w / g.wpp;
-    const uint32_t start = piece != last_piece ? 1u : 0u;
-    last_piece = piece;
-    ent[i] = (w << 2) | (end << 1) | start;
-    if (end) slot_out[w] = i;
-    else slot_in[w] = i;
-    if (start) atomicOr(gstart + (i >> 5), 1u << (i & 31));
+  __syncwarp();
+  if (staged) {
+    for (uint32_t j0 = 0; j0 < span; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      const uint32_t val = j < span ? buf[j] : 0u;
+      if (j < span) ent[lo + j] = val;
+      // the group-start bits of these 32 entries, into their one or two words
+      const uint32_t m = __ballot_sync(0xffffffffu, (val & 1u) != 0u);
+      if (lane == 0 && m) {
+        const uint32_t i0 = lo + j0, sh = i0 & 31u, wd = i0 >> 5;
+        atomicOr(gstart + wd, m << sh);
+        if (sh && (m >> (32 - sh))) atomicOr(gstart + wd + 1, m >> (32 - sh));
+      }
+    }
   }
-  if (locator[x]) atomicOr(off + x, kPrivateBit);
 }
 
 }  // namespace
@@ -383,7 +428,8 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   if (jr) return jr;
   GenArgs g;
   g.P = P; g.npp = npp; g.wpp = wpp;
-  g.pct = p->pct_wire_in_piece; g.L_off = p->L_offset; g.L_scale = p->L_scale;
+  g.pct_thr = drand::pct_threshold(p->pct_wire_in_piece);
+  g.L_off = p->L_offset; g.L_scale = p->L_scale;
   g.seed_state = (((uint64_t)p->random_seed & 0xffffffffull) << 16) | 0x330Eull;
   g.W = W; g.N = N;
 
