@@ -125,32 +125,35 @@ __global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint
                                   uint32_t *count) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
-  const int64_t p0 = base + c * kChunk, p1 = p0 + kChunk;
+  const int64_t p0 = base + c * kChunk;
   uint64_t x = skip(g.seed_state, (uint64_t)p0);
-  int64_t s[7];
-  uint32_t n[7];
+  // positions relative to the chunk start; tracker q's current wire starts
+  // at s[q], and its in-piece draw is s[q] + 4
+  uint32_t s[7], n[7];
 #pragma unroll
   for (int q = 0; q < 7; q++) {
-    s[q] = p0 + q;
+    s[q] = (uint32_t)q;
     n[q] = 0;
   }
-  for (int64_t t = p0; t < p1 + 4; t++) {
-    x = (kA * x + kC) & kMask;  // draw t
-    bool need = false;
+  uint32_t due = 4;  // the next draw some tracker tests
+  for (uint32_t t = 0; t < (uint32_t)kChunk + 4; t++) {
+    next(x);
+    if (t != due) continue;
+    const uint32_t step = crosses(g, x) ? 7u : 6u;
+    due = 0xffffffffu;
 #pragma unroll
-    for (int q = 0; q < 7; q++) need |= (s[q] < p1 && s[q] + 4 == t);
-    if (!need) continue;
-    const bool cr = crosses(g, x);
-#pragma unroll
-    for (int q = 0; q < 7; q++)
-      if (s[q] < p1 && s[q] + 4 == t) {
+    for (int q = 0; q < 7; q++) {
+      if (s[q] < (uint32_t)kChunk && s[q] + 4 == t) {
         n[q]++;
-        s[q] += 6 + (cr ? 1 : 0);
+        s[q] += step;
       }
+      if (s[q] < (uint32_t)kChunk) due = min(due, s[q] + 4);
+    }
+    if (due == 0xffffffffu) break;  // every tracker has left the chunk
   }
 #pragma unroll
   for (int q = 0; q < 7; q++) {
-    exit_phase[c * 7 + q] = (uint8_t)(s[q] - p1);
+    exit_phase[c * 7 + q] = (uint8_t)(s[q] - (uint32_t)kChunk);
     count[c * 7 + q] = n[q];
   }
 }
@@ -216,42 +219,57 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Every chunk emits its wires (circuit.cc:1158-1186).
-__global__ void gen_wires_kernel(GenArgs g, int64_t base, int64_t nchunks,
-                                 const uint8_t *__restrict__ rel_phase,
-                                 const uint32_t *__restrict__ rel_base,
-                                 const uint8_t *__restrict__ bphase,
-                                 const uint64_t *__restrict__ bbase, uint32_t *in_ptr,
-                                 uint32_t *out_ptr, float *L, float *R, float *C,
-                                 int32_t *locator) {
+// Every chunk walks its wires from its entry phase and records where each
+// starts in the draw stream (relative to the first wire draw).
+__global__ void wire_starts_kernel(GenArgs g, int64_t base, int64_t nchunks,
+                                   const uint8_t *__restrict__ rel_phase,
+                                   const uint32_t *__restrict__ rel_base,
+                                   const uint8_t *__restrict__ bphase,
+                                   const uint64_t *__restrict__ bbase, uint32_t *starts) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
   const int64_t b = c / kMapBlock;
   const int qb = bphase[b];  // the block's entry phase selects the chunk's entry
   int64_t w = (int64_t)bbase[b] + rel_base[c * 7 + qb];
   if (w >= g.W) return;
-  const int64_t p0 = base + c * kChunk, p1 = p0 + kChunk;
-  int64_t s = p0 + rel_phase[c * 7 + qb];
-  uint64_t x = skip(g.seed_state, (uint64_t)s);
-  while (s < p1 && w < g.W) {
-    const uint64_t xR = next(x), xL = next(x), xC = next(x), xIn = next(x), xPct = next(x);
-    const uint32_t n = (uint32_t)(w / g.wpp);
-    R[w] = drand::resistance(xR);
-    L[w] = __double2float_rn(__dadd_rn(__dmul_rn(drand::value(xL), g.L_scale), g.L_off));
-    C[w] = __double2float_rn(__dmul_rn(drand::value(xC), 0.1));
-    in_ptr[w] = pick(xIn, n, (uint32_t)g.npp);
-    if (!crosses(g, xPct)) {
-      out_ptr[w] = pick(next(x), n, (uint32_t)g.npp);
-      s += 6;
-    } else {
-      int nn = (int)drand::trunc_mul(next(x), (uint32_t)(g.P - 1));
-      if (nn >= (int)n) nn++;
-      const uint32_t o = pick(next(x), (uint32_t)nn, (uint32_t)g.npp);
-      out_ptr[w] = o;
-      locator[o] = 0;
-      s += 7;
+  const int64_t p0 = base + c * kChunk;
+  uint32_t sr = rel_phase[c * 7 + qb];  // relative to p0
+  uint64_t x = skip(g.seed_state, (uint64_t)p0);
+  uint32_t t = 0;
+  while (sr < (uint32_t)kChunk && w < g.W) {
+    starts[w] = (uint32_t)(c * kChunk + sr);
+    while (t <= sr + 4) {  // advance to the wire's in-piece draw
+      next(x);
+      t++;
     }
+    sr += crosses(g, x) ? 7u : 6u;
     w++;
+  }
+}
+
+// One thread per wire (circuit.cc:1158-1186): jump to its first draw, draw
+// R, L, C, the in-node, the in-piece test and the out-node, and store every
+// field coalesced.
+__global__ void gen_wires_kernel(GenArgs g, int64_t base, const uint32_t *__restrict__ starts,
+                                 uint32_t *in_ptr, uint32_t *out_ptr, float *L, float *R, float *C,
+                                 int32_t *locator) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= g.W) return;
+  uint64_t x = skip(g.seed_state, (uint64_t)(base + starts[w]));
+  const uint64_t xR = next(x), xL = next(x), xC = next(x), xIn = next(x), xPct = next(x);
+  const uint32_t n = (uint32_t)(w / g.wpp);
+  R[w] = drand::resistance(xR);
+  L[w] = __double2float_rn(__dadd_rn(__dmul_rn(drand::value(xL), g.L_scale), g.L_off));
+  C[w] = __double2float_rn(__dmul_rn(drand::value(xC), 0.1));
+  in_ptr[w] = pick(xIn, n, (uint32_t)g.npp);
+  if (!crosses(g, xPct)) {
+    out_ptr[w] = pick(next(x), n, (uint32_t)g.npp);
+  } else {
+    int nn = (int)drand::trunc_mul(next(x), (uint32_t)(g.P - 1));
+    if (nn >= (int)n) nn++;
+    const uint32_t o = pick(next(x), (uint32_t)nn, (uint32_t)g.npp);
+    out_ptr[w] = o;
+    locator[o] = 0;
   }
 }
 
@@ -456,11 +474,11 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   const size_t sz_exit = nchunks * 7, sz_cnt = nchunks * 7 * 4, sz_rph = nchunks * 7,
                sz_rb = nchunks * 7 * 4, sz_bexit = nblocks * 7, sz_bcnt = nblocks * 7 * 4,
                sz_bph = nblocks, sz_bb = nblocks * 8, sz_deg = (N + 1) * 4,
-               sz_sums = (scan_blocks + 1) * 4, sz_tmp = 2 * W * 4;
+               sz_sums = (scan_blocks + 1) * 4, sz_tmp = 2 * W * 4, sz_starts = W * 4;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   const size_t total = al(sz_exit) + al(sz_cnt) + al(sz_rph) + al(sz_rb) + al(sz_bexit) +
                        al(sz_bcnt) + al(sz_bph) + al(sz_bb) + al(sz_deg) + al(sz_sums) +
-                       al(sz_tmp);
+                       al(sz_tmp) + al(sz_starts);
   char *scratch = nullptr;
   CKT_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), total, s));
   char *q = scratch;
@@ -480,6 +498,7 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   uint32_t *deg = (uint32_t *)take(sz_deg);
   uint32_t *sums = (uint32_t *)take(sz_sums);
   uint32_t *tmp = (uint32_t *)take(sz_tmp);
+  uint32_t *starts = (uint32_t *)take(sz_starts);
   int rc = CKT_OK;
   auto ok = [&rc](cudaError_t e) {
     if (rc == CKT_OK && e != cudaSuccess)
@@ -493,9 +512,12 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   ok(cudaGetLastError());
   map_top_kernel<<<1, 256, 0, s>>>(nblocks, bexit, bcount, bphase, bbase);
   ok(cudaGetLastError());
-  gen_wires_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(
-      g, base, nchunks, rel_phase, rel_base, bphase, bbase, o->in_ptr, o->out_ptr,
-      o->inductance, o->resistance, o->capacitance, o->locator);
+  wire_starts_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(g, base, nchunks, rel_phase,
+                                                             rel_base, bphase, bbase, starts);
+  ok(cudaGetLastError());
+  gen_wires_kernel<<<grid_for(W), 256, 0, s>>>(g, base, starts, o->in_ptr, o->out_ptr,
+                                               o->inductance, o->resistance, o->capacitance,
+                                               o->locator);
   ok(cudaGetLastError());
   ok(cudaMemsetAsync(deg, 0, sz_deg, s));
   gen_locs_kernel<<<grid_for(W), 256, 0, s>>>(g, o->in_ptr, o->out_ptr, o->locator, o->in_loc,
