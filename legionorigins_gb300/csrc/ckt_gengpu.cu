@@ -49,7 +49,12 @@ Jump make_jump() {
   return j;
 }
 
-// The jump table never changes: it is copied to each device once.  (A
+// State after k draws, k < kChunk: a[k]*x + c[k], for jumps from a chunk's
+// start to a wire inside it (lanes index it independently, so it lives in
+// global memory, not the constant bank).
+__device__ uint64_t g_near_a[kChunk], g_near_c[kChunk];
+
+// The jump tables never change: they are copied to each device once.  (A
 // per-call copy from pageable memory would wait for the stream's earlier
 // work.)
 constexpr int kMaxDevices = 64;
@@ -64,6 +69,16 @@ int ensure_jump_table() {
   if (!loaded[dev]) {
     const Jump jump = make_jump();
     CKT_CUDA(cudaMemcpyToSymbol(g_jump, &jump, sizeof(Jump)));
+    std::vector<uint64_t> na(kChunk), nc(kChunk);
+    uint64_t a = 1, c = 0;
+    for (int k = 0; k < kChunk; k++) {
+      na[k] = a;
+      nc[k] = c;
+      c = (kA * c + kC) & kMask;  // one more draw: x -> A x + C
+      a = (kA * a) & kMask;
+    }
+    CKT_CUDA(cudaMemcpyToSymbol(g_near_a, na.data(), kChunk * sizeof(uint64_t)));
+    CKT_CUDA(cudaMemcpyToSymbol(g_near_c, nc.data(), kChunk * sizeof(uint64_t)));
     loaded[dev] = true;
   }
   return CKT_OK;
@@ -121,40 +136,36 @@ __global__ void gen_nodes_kernel(GenArgs g, float *charge, float *nvolt, float *
 // its end) and how many wires start inside it.  Only a wire's 5th draw (the
 // in-piece test) matters here, so the state advances for every draw and is
 // converted to a double only where some phase needs that test.
-__global__ void chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint8_t *exit_phase,
-                                  uint32_t *count) {
+constexpr int kChunkWords = (kChunk + 4 + 31) / 32;  // in-piece test bits of a chunk's draws
+constexpr int kMapsBlock = 128;
+
+__global__ void __launch_bounds__(kMapsBlock)
+    chunk_maps_kernel(GenArgs g, int64_t base, int64_t nchunks, uint8_t *exit_phase,
+                      uint32_t *count) {
+  __shared__ uint32_t sbits[kChunkWords][kMapsBlock];
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
-  const int64_t p0 = base + c * kChunk;
-  uint64_t x = skip(g.seed_state, (uint64_t)p0);
-  // positions relative to the chunk start; tracker q's current wire starts
-  // at s[q], and its in-piece draw is s[q] + 4
-  uint32_t s[7], n[7];
+  // 1. the cross-piece test of every draw of the chunk, as bits (the same
+  //    work on every lane)
+  uint64_t x = skip(g.seed_state, (uint64_t)(base + c * kChunk));
+#pragma unroll
+  for (int wd = 0; wd < kChunkWords; wd++) {
+    uint32_t bits = 0;
+    for (int k = 0; k < 32; k++) bits |= (crosses(g, next(x)) ? 1u : 0u) << k;
+    sbits[wd][threadIdx.x] = bits;
+  }
+  // 2. each entry phase hops wire to wire: 6 draws, or 7 when the wire's
+  //    5th draw says it leaves its piece
 #pragma unroll
   for (int q = 0; q < 7; q++) {
-    s[q] = (uint32_t)q;
-    n[q] = 0;
-  }
-  uint32_t due = 4;  // the next draw some tracker tests
-  for (uint32_t t = 0; t < (uint32_t)kChunk + 4; t++) {
-    next(x);
-    if (t != due) continue;
-    const uint32_t step = crosses(g, x) ? 7u : 6u;
-    due = 0xffffffffu;
-#pragma unroll
-    for (int q = 0; q < 7; q++) {
-      if (s[q] < (uint32_t)kChunk && s[q] + 4 == t) {
-        n[q]++;
-        s[q] += step;
-      }
-      if (s[q] < (uint32_t)kChunk) due = min(due, s[q] + 4);
+    uint32_t s = (uint32_t)q, n = 0;
+    while (s < (uint32_t)kChunk) {
+      const uint32_t t = s + 4;
+      s += 6u + ((sbits[t >> 5][threadIdx.x] >> (t & 31u)) & 1u);
+      n++;
     }
-    if (due == 0xffffffffu) break;  // every tracker has left the chunk
-  }
-#pragma unroll
-  for (int q = 0; q < 7; q++) {
-    exit_phase[c * 7 + q] = (uint8_t)(s[q] - (uint32_t)kChunk);
-    count[c * 7 + q] = n[q];
+    exit_phase[c * 7 + q] = (uint8_t)(s - (uint32_t)kChunk);
+    count[c * 7 + q] = n;
   }
 }
 
@@ -225,7 +236,8 @@ __global__ void wire_starts_kernel(GenArgs g, int64_t base, int64_t nchunks,
                                    const uint8_t *__restrict__ rel_phase,
                                    const uint32_t *__restrict__ rel_base,
                                    const uint8_t *__restrict__ bphase,
-                                   const uint64_t *__restrict__ bbase, uint32_t *starts) {
+                                   const uint64_t *__restrict__ bbase, uint32_t *starts,
+                                   uint64_t *chunk_state) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
   const int64_t b = c / kMapBlock;
@@ -235,6 +247,7 @@ __global__ void wire_starts_kernel(GenArgs g, int64_t base, int64_t nchunks,
   const int64_t p0 = base + c * kChunk;
   uint32_t sr = rel_phase[c * 7 + qb];  // relative to p0
   uint64_t x = skip(g.seed_state, (uint64_t)p0);
+  chunk_state[c] = x;
   uint32_t t = 0;
   while (sr < (uint32_t)kChunk && w < g.W) {
     starts[w] = (uint32_t)(c * kChunk + sr);
@@ -250,12 +263,15 @@ __global__ void wire_starts_kernel(GenArgs g, int64_t base, int64_t nchunks,
 // One thread per wire (circuit.cc:1158-1186): jump to its first draw, draw
 // R, L, C, the in-node, the in-piece test and the out-node, and store every
 // field coalesced.
-__global__ void gen_wires_kernel(GenArgs g, int64_t base, const uint32_t *__restrict__ starts,
-                                 uint32_t *in_ptr, uint32_t *out_ptr, float *L, float *R, float *C,
+__global__ void gen_wires_kernel(GenArgs g, const uint32_t *__restrict__ starts,
+                                 const uint64_t *__restrict__ chunk_state, uint32_t *in_ptr,
+                                 uint32_t *out_ptr, float *L, float *R, float *C,
                                  int32_t *locator) {
   const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= g.W) return;
-  uint64_t x = skip(g.seed_state, (uint64_t)(base + starts[w]));
+  const uint32_t st = starts[w], k = st % (uint32_t)kChunk;
+  uint64_t x = (__ldg(g_near_a + k) * chunk_state[st / (uint32_t)kChunk] + __ldg(g_near_c + k)) &
+               kMask;
   const uint64_t xR = next(x), xL = next(x), xC = next(x), xIn = next(x), xPct = next(x);
   const uint32_t n = (uint32_t)(w / g.wpp);
   R[w] = drand::resistance(xR);
@@ -474,11 +490,12 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   const size_t sz_exit = nchunks * 7, sz_cnt = nchunks * 7 * 4, sz_rph = nchunks * 7,
                sz_rb = nchunks * 7 * 4, sz_bexit = nblocks * 7, sz_bcnt = nblocks * 7 * 4,
                sz_bph = nblocks, sz_bb = nblocks * 8, sz_deg = (N + 1) * 4,
-               sz_sums = (scan_blocks + 1) * 4, sz_tmp = 2 * W * 4, sz_starts = W * 4;
+               sz_sums = (scan_blocks + 1) * 4, sz_tmp = 2 * W * 4, sz_starts = W * 4,
+               sz_cstate = nchunks * 8;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   const size_t total = al(sz_exit) + al(sz_cnt) + al(sz_rph) + al(sz_rb) + al(sz_bexit) +
                        al(sz_bcnt) + al(sz_bph) + al(sz_bb) + al(sz_deg) + al(sz_sums) +
-                       al(sz_tmp) + al(sz_starts);
+                       al(sz_tmp) + al(sz_starts) + al(sz_cstate);
   char *scratch = nullptr;
   CKT_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&scratch), total, s));
   char *q = scratch;
@@ -499,23 +516,25 @@ extern "C" int ckt_generate_device(const ckt_gen_params *p, ckt_device_circuit *
   uint32_t *sums = (uint32_t *)take(sz_sums);
   uint32_t *tmp = (uint32_t *)take(sz_tmp);
   uint32_t *starts = (uint32_t *)take(sz_starts);
+  uint64_t *chunk_state = (uint64_t *)take(sz_cstate);
   int rc = CKT_OK;
   auto ok = [&rc](cudaError_t e) {
     if (rc == CKT_OK && e != cudaSuccess)
       rc = set_error(CKT_ECUDA, "device generator: %s", cudaGetErrorString(e));
   };
 
-  chunk_maps_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(g, base, nchunks, exit_phase, count);
+  chunk_maps_kernel<<<grid_for(nchunks, kMapsBlock), kMapsBlock, 0, s>>>(g, base, nchunks,
+                                                                          exit_phase, count);
   ok(cudaGetLastError());
   map_block_kernel<<<(unsigned)nblocks, 128, 0, s>>>(nchunks, exit_phase, count, rel_phase,
                                                       rel_base, bexit, bcount);
   ok(cudaGetLastError());
   map_top_kernel<<<1, 256, 0, s>>>(nblocks, bexit, bcount, bphase, bbase);
   ok(cudaGetLastError());
-  wire_starts_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(g, base, nchunks, rel_phase,
-                                                             rel_base, bphase, bbase, starts);
+  wire_starts_kernel<<<grid_for(nchunks, 128), 128, 0, s>>>(
+      g, base, nchunks, rel_phase, rel_base, bphase, bbase, starts, chunk_state);
   ok(cudaGetLastError());
-  gen_wires_kernel<<<grid_for(W), 256, 0, s>>>(g, base, starts, o->in_ptr, o->out_ptr,
+  gen_wires_kernel<<<grid_for(W), 256, 0, s>>>(g, starts, chunk_state, o->in_ptr, o->out_ptr,
                                                o->inductance, o->resistance, o->capacitance,
                                                o->locator);
   ok(cudaGetLastError());
