@@ -38,7 +38,9 @@ struct Job {
   int status = CKT_OK;
   bool cancel = false;
   double submit_s = 0, admit_s = 0, start_s = -1, finish_s = 0;
-  int32_t loops_done = 0;
+  int32_t loops_done = 0;      // rounds completed
+  int32_t loops_enqueued = 0;  // rounds launched (completed or in flight)
+  int fail = CKT_OK;           // status of a failed round this job was in
   // host data (prep output)
   std::vector<uint32_t> in_ptr, out_ptr, slot_in, slot_out, ent, off, gstart;
   std::vector<uint8_t> in_loc, out_loc;
@@ -95,6 +97,16 @@ struct ckt_server {
   size_t circ_cap = 0;
   uint32_t *d_sync = nullptr;
   size_t sync_cap = 0;
+  // Two rounds may be in flight on the compute stream; each has its own
+  // pinned host copy of its tables and error word, and timing events.
+  struct Stage {
+    BatchItem *items = nullptr;
+    size_t items_cap = 0;
+    RoundCircuit *circ = nullptr;
+    size_t circ_cap = 0;
+    uint32_t *err = nullptr;
+    cudaEvent_t start = nullptr, end = nullptr;
+  } stage[2];
   std::vector<std::thread> prep_threads;
   std::thread io_thread, sched_thread;
 
@@ -364,17 +376,109 @@ int ensure_cap(T **p, size_t *cap, size_t need) {
   return CKT_OK;
 }
 
+template <typename T>
+int ensure_host_cap(T **p, size_t *cap, size_t need) {
+  if (*cap >= need) return CKT_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  const size_t n = std::max<size_t>(need * 2, 64);
+  CKT_CUDA(cudaMallocHost(reinterpret_cast<void **>(p), n * sizeof(T)));
+  *cap = n;
+  return CKT_OK;
+}
+
+// A round launched on the compute stream and not yet retired.
+struct InFlight {
+  int slot;
+  std::vector<std::shared_ptr<Job>> jobs;
+};
+
+// Sends a job whose rounds are all retired to the IO thread (download,
+// release) when it is finished, cancelled or failed.  Called with s->mu held.
+void maybe_drain(ckt_server *s, const std::shared_ptr<Job> &j) {
+  if (j->state != kResident || j->loops_enqueued != j->loops_done) return;
+  if (!(j->fail || j->cancel || j->loops_done >= j->req.loops)) return;
+  s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), j), s->resident.end());
+  if (j->fail) j->status = j->fail;
+  else if (j->loops_done < j->req.loops) j->status = CKT_ECANCELLED;
+  j->state = kDraining;
+  s->io_down.push_back(j);
+}
+
+// Retires the oldest round: waits for its end event, reads its error word,
+// advances its jobs.
+void retire_round(ckt_server *s, InFlight &f) {
+  ckt_server::Stage &st = s->stage[f.slot];
+  int rc = cudaEventSynchronize(st.end) == cudaSuccess ? CKT_OK : CKT_ECUDA;
+  if (rc) set_error(CKT_ECUDA, "round failed: %s", cudaGetErrorString(cudaGetLastError()));
+  else if (*st.err) rc = set_error(CKT_ETIMEOUT, "a round's bounded wait ran out");
+  float ms = 0.f;
+  if (!rc) cudaEventElapsedTime(&ms, st.start, st.end);
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->rounds++;
+  s->busy_s += 1e-3 * ms;
+  for (auto &j : f.jobs) {
+    j->loops_done++;
+    if (rc && !j->fail) j->fail = rc;
+    maybe_drain(s, j);
+  }
+  s->cv_io.notify_all();
+}
+
+// Builds and launches one round over `jobs` into stage `slot`.  Buffers that
+// must grow are grown only with no round in flight (the caller retires them
+// first when grow_needed says so).
+bool grow_needed(const ckt_server *s, int slot, size_t nitems, size_t ncirc) {
+  const ckt_server::Stage &st = s->stage[slot];
+  return nitems > s->items_cap || ncirc > s->circ_cap || 2 + 2 * ncirc > s->sync_cap ||
+         nitems > st.items_cap || ncirc > st.circ_cap || st.err == nullptr;
+}
+
+int launch_staged_round(ckt_server *s, int slot, const std::vector<RoundCircuit> &circ,
+                        const std::vector<BatchItem> &items) {
+  ckt_server::Stage &st = s->stage[slot];
+  int rc;
+  if ((rc = ensure_cap(&s->d_items, &s->items_cap, std::max<size_t>(items.size(), 1))) ||
+      (rc = ensure_cap(&s->d_circ, &s->circ_cap, circ.size())) ||
+      (rc = ensure_cap(&s->d_sync, &s->sync_cap, 2 + 2 * circ.size())) ||
+      (rc = ensure_host_cap(&st.items, &st.items_cap, std::max<size_t>(items.size(), 1))) ||
+      (rc = ensure_host_cap(&st.circ, &st.circ_cap, circ.size())))
+    return rc;
+  if (!st.err) CKT_CUDA(cudaMallocHost(reinterpret_cast<void **>(&st.err), sizeof(uint32_t)));
+  memcpy(st.items, items.data(), items.size() * sizeof(BatchItem));
+  memcpy(st.circ, circ.data(), circ.size() * sizeof(RoundCircuit));
+  *st.err = 0;
+  CKT_CUDA(cudaEventRecord(st.start, s->compute));
+  CKT_CUDA(cudaMemcpyAsync(s->d_items, st.items, items.size() * sizeof(BatchItem),
+                           cudaMemcpyHostToDevice, s->compute));
+  CKT_CUDA(cudaMemcpyAsync(s->d_circ, st.circ, circ.size() * sizeof(RoundCircuit),
+                           cudaMemcpyHostToDevice, s->compute));
+  if ((rc = launch_round(s->cfg.mode, s->cfg.launch, s->grid, s->d_items, (uint32_t)items.size(),
+                         s->d_circ, (uint32_t)circ.size(), s->d_sync, s->cfg.round_timeout_ns,
+                         s->compute)))
+    return rc;
+  CKT_CUDA(cudaMemcpyAsync(st.err, s->d_sync + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           s->compute));
+  CKT_CUDA(cudaEventRecord(st.end, s->compute));
+  return CKT_OK;
+}
+
+// The scheduler keeps up to two rounds in flight: the next round's members
+// are known before the current one ends (every resident circuit with loops
+// left, plus circuits whose upload has finished), so it is launched right
+// behind it on the stream and the GPU does not wait for the host between
+// rounds.  Circuits join and leave at round boundaries.
 void sched_loop(ckt_server *s) {
   cudaSetDevice(s->device);
-  std::vector<std::shared_ptr<Job>> active;
+  std::deque<InFlight> inflight;
   std::vector<RoundCircuit> circ;
   std::vector<BatchItem> items;
-  cudaEvent_t round_done;
-  cudaEventCreateWithFlags(&round_done, cudaEventDisableTiming);
+  int slot = 0;
   while (true) {
-    active.clear();
+    std::vector<std::shared_ptr<Job>> next;
     {
       std::unique_lock<std::mutex> lk(s->mu);
+      if (s->stop) break;
       // Admission: prepared requests, first come first served, while slots
       // and the HBM budget allow.  A request larger than the whole budget
       // can never run: it completes with CKT_ENOMEM.
@@ -403,70 +507,59 @@ void sched_loop(ckt_server *s) {
         s->io_up.push_back(j);
         s->cv_io.notify_all();
       }
-      for (auto &j : s->resident)
-        if (j->state == kResident && j->uploaded && cudaEventQuery(j->uploaded) == cudaSuccess)
-          active.push_back(j);
-      if (s->stop) break;
-      if (active.empty()) {
+      const std::vector<std::shared_ptr<Job>> res = s->resident;
+      for (auto &j : res) {
+        if (j->state != kResident || !j->uploaded) continue;
+        if (j->loops_enqueued == 0 && cudaEventQuery(j->uploaded) != cudaSuccess) continue;
+        maybe_drain(s, j);  // cancelled or failed with nothing in flight
+        if (j->state == kResident && !j->fail && !j->cancel && j->loops_enqueued < j->req.loops)
+          next.push_back(j);
+      }
+      s->cv_io.notify_all();
+      if (next.empty() && inflight.empty()) {
         s->cv_sched.wait_for(lk, std::chrono::microseconds(200));
         continue;
       }
     }
-    // One round over the active set.
-    NvtxRange range("ckt_server_round");
-    circ.resize(active.size());
-    for (size_t k = 0; k < active.size(); k++) {
-      circ[k] = active[k]->rc;
-      if (active[k]->start_s < 0) active[k]->start_s = s->now();
+    if (next.empty() || inflight.size() >= 2) {
+      retire_round(s, inflight.front());
+      inflight.pop_front();
+      continue;
     }
+    circ.resize(next.size());
+    for (size_t k = 0; k < next.size(); k++) circ[k] = next[k]->rc;
     build_round_table(circ, s->cfg.launch, items);
-    const double t_round = s->now();
-    int rc = ensure_cap(&s->d_items, &s->items_cap, std::max<size_t>(items.size(), 1));
-    if (!rc) rc = ensure_cap(&s->d_circ, &s->circ_cap, circ.size());
-    if (!rc) rc = ensure_cap(&s->d_sync, &s->sync_cap, 2 + 2 * circ.size());
-    if (!rc && !items.empty())
-      rc = cudaMemcpyAsync(s->d_items, items.data(), items.size() * sizeof(BatchItem),
-                           cudaMemcpyHostToDevice, s->compute) == cudaSuccess ? CKT_OK : CKT_ECUDA;
-    if (!rc)
-      rc = cudaMemcpyAsync(s->d_circ, circ.data(), circ.size() * sizeof(RoundCircuit),
-                           cudaMemcpyHostToDevice, s->compute) == cudaSuccess ? CKT_OK : CKT_ECUDA;
-    if (!rc && !items.empty())
-      rc = launch_round(s->cfg.mode, s->cfg.launch, s->grid, s->d_items, (uint32_t)items.size(),
-                        s->d_circ, (uint32_t)circ.size(), s->d_sync, s->cfg.round_timeout_ns,
-                        s->compute);
-    uint32_t err = 0;
-    if (!rc)
-      rc = cudaMemcpyAsync(&err, s->d_sync + 1, 4, cudaMemcpyDeviceToHost, s->compute) == cudaSuccess
-               ? CKT_OK : CKT_ECUDA;
-    if (!rc) {
-      cudaEventRecord(round_done, s->compute);
-      rc = cudaEventSynchronize(round_done) == cudaSuccess ? CKT_OK : CKT_ECUDA;
+    if (grow_needed(s, slot, items.size(), circ.size()) && !inflight.empty()) {
+      // buffers are reallocated only with nothing in flight
+      while (!inflight.empty()) {
+        retire_round(s, inflight.front());
+        inflight.pop_front();
+      }
+      continue;  // membership may have changed
     }
-    if (!rc && err) rc = CKT_ETIMEOUT;
+    NvtxRange range("ckt_server_round");
+    const int rc = items.empty() ? CKT_OK : launch_staged_round(s, slot, circ, items);
     std::lock_guard<std::mutex> lk(s->mu);
-    s->rounds++;
-    s->busy_s += s->now() - t_round;
-    for (auto &j : active) {
+    const double t = s->now();
+    for (auto &j : next) {
       if (rc) {
-        s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), j),
-                          s->resident.end());
-        j->state = kDraining;
-        j->status = rc;
-        s->io_down.push_back(j);
+        j->fail = rc;
+        maybe_drain(s, j);
         continue;
       }
-      j->loops_done++;
-      if (j->loops_done >= j->req.loops || j->cancel) {
-        s->resident.erase(std::remove(s->resident.begin(), s->resident.end(), j),
-                          s->resident.end());
-        if (j->loops_done < j->req.loops) j->status = CKT_ECANCELLED;
-        j->state = kDraining;
-        s->io_down.push_back(j);
+      if (j->start_s < 0) j->start_s = t;
+      j->loops_enqueued++;
+      if (items.empty()) {  // nothing to run: the round is done already
+        j->loops_done++;
+        maybe_drain(s, j);
       }
+    }
+    if (!rc && !items.empty()) {
+      inflight.push_back({slot, next});
+      slot ^= 1;
     }
     s->cv_io.notify_all();
   }
-  cudaEventDestroy(round_done);
 }
 
 }  // namespace
@@ -508,6 +601,10 @@ int ckt_server_create(const ckt_server_config *cfg, ckt_server **out) {
   s->grid = s->sm_count * per_sm;
   CKT_CUDA(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking));
   CKT_CUDA(cudaStreamCreateWithFlags(&s->io, cudaStreamNonBlocking));
+  for (auto &st : s->stage) {
+    CKT_CUDA(cudaEventCreate(&st.start));
+    CKT_CUDA(cudaEventCreate(&st.end));
+  }
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
     uint64_t keep = UINT64_MAX;
@@ -634,6 +731,13 @@ int ckt_server_destroy(ckt_server *s) {
   cudaFree(s->d_items);
   cudaFree(s->d_circ);
   cudaFree(s->d_sync);
+  for (auto &st : s->stage) {
+    if (st.items) cudaFreeHost(st.items);
+    if (st.circ) cudaFreeHost(st.circ);
+    if (st.err) cudaFreeHost(st.err);
+    if (st.start) cudaEventDestroy(st.start);
+    if (st.end) cudaEventDestroy(st.end);
+  }
   cudaStreamDestroy(s->compute);
   cudaStreamDestroy(s->io);
   delete s;
