@@ -276,6 +276,9 @@ def main() -> None:
                          "(default: the library's)")
     ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
                     help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
+    ap.add_argument("--circuits", type=int, default=256,
+                    help="batched: number of circuits of the mix (256 for the benchmark; fewer "
+                         "only to profile)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -567,7 +570,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     from legionorigins_gb300.batch import Batch
     from legionorigins_gb300.workloads import mixed_batch
 
-    specs = mixed_batch(256)
+    specs = mixed_batch(args.circuits)
     t_build = time.perf_counter()
     b = Batch(specs, threads=cpu_threads())
     t_build = time.perf_counter() - t_build
@@ -695,7 +698,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (reference generator distributions, seeds 0..255)",
             "config": {
-                "workload": "batched mixed sizes: 256 independent circuits, pieces U{1..32}, "
+                "workload": f"batched mixed sizes: {len(specs)} independent circuits, pieces U{{1..32}}, "
                             "nodes/piece log-uniform [256,16384], 4 wires/node, in-piece "
                             "U[0.8,0.98], inner steps U{100..1000}, 1 outer loop; one "
                             "persistent launch per step (CUDA graph)",
