@@ -226,6 +226,53 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def accuracy_check(torch, G, C, mode) -> dict:
+    """Max and RMS relative error of the GPU loop against the fp64 oracle on
+    the config-0 circuit in the finite regime (4 inner steps x 2 loops), and
+    NaN/+-Inf/finite class agreement with the fp32 oracle at the configured
+    1000 inner steps x 5 loops (where the reference recurrence overflows)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ckt_oracle as O
+
+    O.build()
+    p = O.GenParams(4, 256, 1024, PCT, SEED, L_offset=L_OFFSET, L_scale=L_SCALE)
+    base = O.generate(p)
+    fields = ("in_ptr", "out_ptr", "in_loc", "out_loc", "L", "R", "C", "current", "voltage",
+              "charge", "node_voltage", "cap", "leak", "locator")
+    state = ("current", "voltage", "charge", "node_voltage")
+
+    def gpu(steps, loops):
+        dc = C.DeviceCircuit({k: np.ascontiguousarray(getattr(base, k)) for k in fields},
+                             C.Shape(4, 256, 1024))
+        dc.run_loops(C.params(steps, mode), loops)
+        torch.cuda.synchronize()
+        out = dc.to_host()
+        dc.close()
+        return out
+
+    def cls(a):
+        return np.where(np.isnan(a), 0, np.where(np.isposinf(a), 1, np.where(np.isneginf(a), 2, 3)))
+
+    got = gpu(4, 2)
+    ref64 = base.astype(np.float64)
+    O.simulate(ref64, 2, 4)
+    rel = np.concatenate([(np.abs(got[k].astype(np.float64) - getattr(ref64, k)) /
+                           np.maximum(np.abs(getattr(ref64, k)), 1e-6)).ravel() for k in state])
+    got_s = gpu(1000, 5)
+    ref32 = base.copy()
+    O.simulate(ref32, 5, 1000)
+    same = sum(int((cls(got_s[k]) == cls(getattr(ref32, k))).sum()) for k in state)
+    total = sum(got_s[k].size for k in state)
+    return {"finite_regime": {"circuit": "4 x 256 x 1024 (config 0 shape)", "inner_steps": 4,
+                              "loops": 2, "max_rel_err_vs_fp64": float(rel.max()),
+                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2)))},
+            "configured_steps": {"inner_steps": 1000, "loops": 5,
+                                 "class_match_vs_fp32_oracle": same / total,
+                                 "elements": total,
+                                 "finite_elements": int(sum(np.isfinite(got_s[k]).sum()
+                                                            for k in state))}}
+
+
 def fp32_peak(torch, G, stream) -> dict:
     """Measured FP32 FMA throughput (FLOP/s) of this GPU, best of 5, with
     single and with paired (f32x2) FMAs; the roofline uses the larger."""
@@ -334,6 +381,13 @@ def main() -> None:
                       f"pieces ({pieces * p.wires_per_piece} wires), reference CPU tasks "
                       f"restated in C (oracle/ckt_oracle.c), {threads} threads",
         }
+
+    # Accuracy of the arithmetic this run uses, stated with the number (the
+    # oracle as the checker, in the CPU leg): the library's loop on the
+    # config-0 circuit (4 x 256 x 1024) against the fp64 and fp32 oracles.
+    accuracy = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        accuracy = accuracy_check(torch, G, C, mode)
 
     shape = C.Shape(args.pieces, SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"])
     host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
@@ -553,6 +607,7 @@ def main() -> None:
             "config": workload_config(args.mode, shape.num_pieces), "roofline": roofline,
             "cpu_baseline": cpu_baseline, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "kernels": kernels, "index_space_tasks": index_space_tasks,
+            "accuracy": accuracy,
             "replicas": "one independent circuit per GPU" if ws > 1 else None,
         }
         print(json.dumps(line), flush=True)
