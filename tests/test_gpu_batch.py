@@ -23,6 +23,7 @@ def small_specs():
         CircuitSpec(6, 40, 100, 83.5, 12, 2),     # real-valued pct
         CircuitSpec(5, 33, 0, 95.0, 13, 3),       # no wires at all
         CircuitSpec(16, 128, 512, 50.0, 14, 1),   # heavy reduction
+        CircuitSpec(2, 1, 5000, 50.0, 15, 2),     # hub nodes: runs over several staging chunks
     ]
 
 

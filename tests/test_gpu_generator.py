@@ -18,6 +18,8 @@ SHAPES = [
     (3, 4, 0, 95.0, 1),            # no wires
     (16, 4096, 16384, 95.0, 42),   # many chunks of the draw stream
     (32, 777, 3001, 83.25, 77),    # real-valued pct, odd sizes
+    (2, 1, 5000, 50.0, 3),         # hub nodes: a warp's span exceeds the sort stage
+    (1, 3, 20000, 95.0, 9),        # one piece, three nodes
 ]
 
 

@@ -129,6 +129,25 @@ def test_per_piece_calls_equal_index_space(cuda, oracle, shape):
         assert same_bits(a[k], getattr(c, k)), k
 
 
+@pytest.mark.parametrize("shape", [(2, 1, 5000, 50, 3), (3, 2, 9000, 0, 4), (1, 1, 3000, 95, 5)],
+                         ids=lambda s: "x".join(str(v) for v in s))
+def test_hub_nodes_exact(cuda, oracle, shape):
+    """One or two nodes per piece and thousands of wires: a node's run spans
+    several staging chunks of distribute_charge (more than 4096 entries)."""
+    c = oracle.generate(oracle.GenParams(*shape, L_offset=0.001))
+    a = run_gpu(cuda, device(cuda, c), 2, 2, mode=0)
+    b = run_gpu(cuda, device(cuda, c), 2, 2, mode=0, per_piece=True)
+    d = device(cuda, c)
+    from legionorigins_gb300 import circuit as C
+    d.run_loops(C.params(2, 0), 2)
+    cuda.cuda.synchronize()
+    f = d.to_host()
+    oracle.simulate(c, 2, 2)
+    for k in STATE:
+        for got in (a, b, f):
+            assert same_bits(got[k], getattr(c, k)), k
+
+
 @pytest.mark.parametrize("P", [1, 2, 4])
 @pytest.mark.parametrize("npp", [1, 2, 3])
 @pytest.mark.parametrize("wpp", [1, 3, 8])
