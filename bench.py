@@ -318,6 +318,8 @@ def main() -> None:
                     help="serve: offered request rates (requests/s) to sweep")
     ap.add_argument("--serve-seconds", type=float, default=6.0,
                     help="serve: seconds of arrivals per rate")
+    ap.add_argument("--serve-plain-sample", type=int, default=48,
+                    help="serve: requests of the stream also timed through the plain path")
     ap.add_argument("--serve-launch", default="",
                     help="serve: round launch shape block,wires_per_thread,dc_schedule "
                          "(default: the library's)")
@@ -1121,6 +1123,36 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
             "rounds": st["rounds"], "resident_peak": st["resident_peak"],
             "hbm_peak_gb": st["bytes_peak"] / 1e9, "gpu_busy_s": st["busy_s"],
         })
+    # The same request stream through the plain path, one request at a time
+    # (circuit already resident, only its loops timed): index-space launches,
+    # and the reference's per-piece task calls with a device wait after each.
+    from legionorigins_gb300 import circuit as C
+
+    plain = {"index_space": [0, 0.0], "per_piece_blocking": [0, 0.0]}
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    for rid in range(args.serve_plain_sample):
+        spec = serve_request(rid)
+        host = C.generate(*spec.gen_args())
+        shape = C.Shape(spec.num_pieces, spec.nodes_per_piece, spec.wires_per_piece)
+        dc = C.DeviceCircuit(host, shape)
+        prm = C.params(spec.steps, mode)
+        torch.cuda.synchronize()
+        for name, acc in plain.items():
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(spec.loops):
+                if name == "index_space":
+                    dc.loop_index_space(prm, sp)
+                else:
+                    dc.loop_per_piece(prm, sp, blocking=True)
+            b.record(stream)
+            b.synchronize()
+            acc[0] += spec.segment_updates  # wires x 10 x steps x loops
+            acc[1] += a.elapsed_time(b) * 1e-3
+        dc.close()
+        del dc
+    plain_rates = {k: (v[0] / v[1] if v[1] > 0 else None) for k, v in plain.items()}
     best = max(sweep, key=lambda r: r["throughput"])
     # latency is quoted at the highest offered rate the server keeps up with
     # (completes >= 95% of the offered rate); above it queueing dominates
@@ -1144,6 +1176,14 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
             "latency_ms": quiet["latency_ms"], "latency_at_offered_rps": quiet["offered_rps"],
             "throughput_at_that_rate": quiet["throughput"],
             "capacity_offered_rps": best["offered_rps"], "sweep": sweep,
+            "plain_sequential": {
+                "requests": args.serve_plain_sample,
+                **{k: {"value": v, "unit": UNIT,
+                       "served_over_it": (best["throughput"] / v) if v else None}
+                   for k, v in plain_rates.items()},
+                "note": "requests 0..n-1 of the stream, one at a time, circuit resident, "
+                        "only their loops timed (device events): the plain path's best case",
+            },
             "e2e": {"value": best["throughput"], "unit": UNIT, "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": None,
                     "note": "serving is end to end by construction: each request is submitted "
