@@ -145,6 +145,9 @@ SIGNATURES = {
     "ckt_graph_destroy": (ctypes.c_int, [_P]),
     "ckt_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                       ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
+    "ckt_graph_tile_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32),
+                                           ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                                           ctypes.POINTER(ctypes.c_uint32)]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
     "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
     "ckt_hist_default_params": (None, [ctypes.POINTER(HistParams)]),

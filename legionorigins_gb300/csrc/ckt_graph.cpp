@@ -15,6 +15,7 @@
 //     order here.
 #include <algorithm>
 #include <cstring>
+#include <thread>
 
 #include "ckt_internal.h"
 
@@ -42,6 +43,11 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->slot_out);
   cudaFree(g->gstart);
   cudaFree(g->contrib);
+  cudaFree(g->tile_step);
+  cudaFree(g->tile_steps);
+  cudaFree(g->tile_ent);
+  cudaFree(g->tile_gw);
+  cudaFree(g->tile_error);
   delete g;
 }
 
@@ -140,6 +146,134 @@ int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nod
   return CKT_OK;
 }
 
+// Tiled distribute_charge plan of one node tile (encoding in ckt_internal.h).
+namespace {
+
+struct TilePlan {
+  std::vector<uint4> steps;  // entry and gather-wire offsets local to the tile
+  std::vector<uint32_t> ent, gw;
+};
+
+// A chunk with at least this many of the tile's contributions is copied
+// whole (16 KB of I[0]/I[9]); sparser chunks are gathered entry by entry,
+// each gather costing a 32-byte sector.
+constexpr uint32_t kDenseMin = kChunkWires / 8;
+
+void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t xe,
+               TilePlan &tp, std::vector<uint64_t> &keys, std::vector<uint64_t> &sparse) {
+  // Key (chunk, node within tile, CSR position): sorted, each node's
+  // contributions stay in CSR (= wire) order inside every chunk.
+  const uint32_t lo = off[x0] & kOffsetMask;
+  keys.clear();
+  for (uint32_t x = x0; x < xe; x++) {
+    const uint32_t b = off[x] & kOffsetMask, e = off[x + 1] & kOffsetMask;
+    for (uint32_t i = b; i < e; i++)
+      keys.push_back(((uint64_t)((ent[i] >> 2) / kChunkWires) << 45) |
+                     ((uint64_t)(x - x0) << 32) | (i - lo));
+  }
+  std::sort(keys.begin(), keys.end());
+
+  auto word = [&](uint64_t key, bool head) -> uint32_t {
+    const uint32_t xl = (uint32_t)(key >> 32) & (kTileNodesMax - 1);
+    const uint32_t i = lo + (uint32_t)key, x = x0 + xl;
+    const uint32_t u = ent[i], w = u >> 2;
+    const bool priv = (off[x] & kPrivateBit) != 0;
+    const bool flush = !priv && (u & 1u) && i != (off[x] & kOffsetMask);
+    return (w % kChunkWires) | ((u & 2u) ? kTeEnd : 0u) | (xl << kTeNodeShift) |
+           (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u);
+  };
+  // Emits [a, b) of `v` (sorted by node, then CSR position) as one step.
+  auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
+    const bool gather = chunk == kGatherStep;
+    const uint32_t e0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
+    uint32_t prev = 0xffffffffu;
+    for (size_t j = a; j < b; j++) {
+      const uint32_t xl = (uint32_t)(v[j] >> 32) & (kTileNodesMax - 1);
+      tp.ent.push_back(word(v[j], xl != prev));
+      if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
+      prev = xl;
+    }
+    while (tp.ent.size() % 4) {  // 16-byte runs for the bulk copies
+      tp.ent.push_back(kTePad);
+      if (gather) tp.gw.push_back(0u);
+    }
+    tp.steps.push_back(make_uint4(e0, (uint32_t)tp.ent.size() - e0, chunk, g0));
+  };
+  auto flush_sparse = [&]() {
+    if (sparse.empty()) return;
+    // One wire range: order by (node, CSR position) only.
+    for (uint64_t &k : sparse) k &= (1ull << 45) - 1;
+    std::sort(sparse.begin(), sparse.end());
+    constexpr size_t kMax = kStepEntriesMax - 4;
+    for (size_t a = 0; a < sparse.size(); a += kMax)
+      emit(sparse, a, std::min(sparse.size(), a + kMax), kGatherStep);
+    sparse.clear();
+  };
+  sparse.clear();
+  for (size_t a = 0; a < keys.size();) {
+    const uint64_t chunk = keys[a] >> 45;
+    size_t b = a;
+    while (b < keys.size() && (keys[b] >> 45) == chunk) b++;
+    if (b - a >= kDenseMin) {
+      flush_sparse();
+      emit(keys, a, b, (uint32_t)chunk);
+    } else {
+      sparse.insert(sparse.end(), keys.begin() + a, keys.begin() + b);
+    }
+    a = b;
+  }
+  flush_sparse();
+}
+
+}  // namespace
+
+// Builds and uploads the tiled distribute_charge plan; tiles are planned
+// in parallel.
+static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
+                           const std::vector<uint32_t> &ent, uint32_t tile_nodes) {
+  // Tile bases and node counts stay 32-bit in the kernel.
+  if (g->N > 0x7fffffff || g->W == 0) return CKT_OK;
+  const uint32_t N = (uint32_t)g->N;
+  const uint32_t T = (N + tile_nodes - 1) / tile_nodes;
+  std::vector<TilePlan> plans(T);
+  const int nthr = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+  std::vector<std::thread> pool;
+  for (int r = 0; r < nthr; r++)
+    pool.emplace_back([&, r]() {
+      std::vector<uint64_t> keys, sparse;
+      for (uint32_t t = (uint32_t)r; t < T; t += (uint32_t)nthr)
+        plan_tile(off.data(), ent.data(), t * tile_nodes, std::min(N, (t + 1) * tile_nodes),
+                  plans[t], keys, sparse);
+    });
+  for (auto &th : pool) th.join();
+  std::vector<uint32_t> tile_step(T + 1, 0), all_ent, all_gw;
+  std::vector<uint4> steps;
+  for (uint32_t t = 0; t < T; t++) {
+    tile_step[t] = (uint32_t)steps.size();
+    const uint32_t eb = (uint32_t)all_ent.size(), gb = (uint32_t)all_gw.size();
+    for (uint4 s : plans[t].steps) steps.push_back(make_uint4(s.x + eb, s.y, s.z, s.w + gb));
+    all_ent.insert(all_ent.end(), plans[t].ent.begin(), plans[t].ent.end());
+    all_gw.insert(all_gw.end(), plans[t].gw.begin(), plans[t].gw.end());
+    std::vector<uint4>().swap(plans[t].steps);
+    std::vector<uint32_t>().swap(plans[t].ent);
+    std::vector<uint32_t>().swap(plans[t].gw);
+  }
+  tile_step[T] = (uint32_t)steps.size();
+  int rc;
+  if ((rc = upload(&g->tile_step, tile_step, &g->device_bytes)) ||
+      (rc = upload(&g->tile_steps, steps, &g->device_bytes)) ||
+      (rc = upload(&g->tile_ent, all_ent, &g->device_bytes)) ||
+      (rc = upload(&g->tile_gw, all_gw, &g->device_bytes)) ||
+      (rc = upload(&g->tile_error, std::vector<uint32_t>(1, 0u), &g->device_bytes)))
+    return rc;
+  g->tile_nodes = tile_nodes;
+  g->num_tiles = T;
+  g->tile_num_steps = (int64_t)steps.size();
+  g->tile_stream_steps = 0;
+  for (const uint4 &s : steps) g->tile_stream_steps += s.z != kGatherStep;
+  return CKT_OK;
+}
+
 }  // namespace ckt
 
 extern "C" {
@@ -208,7 +342,8 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
       (rc = upload(&g->slot_in, slot_in, &g->device_bytes)) ||
       (rc = upload(&g->slot_out, slot_out, &g->device_bytes)) ||
       (rc = upload(&g->gstart, gstart, &g->device_bytes)) ||
-      (rc = upload(&g->contrib, std::vector<float>(2 * W), &g->device_bytes))) {
+      (rc = upload(&g->contrib, std::vector<float>(2 * W), &g->device_bytes)) ||
+      (rc = build_tile_plan(g, off, ent, kTileNodesMax))) {
     free_graph(g);
     return rc;
   }
@@ -243,6 +378,20 @@ int ckt_graph_info(const ckt_graph *g, int64_t *num_wires, int64_t *num_nodes,
   if (num_nodes) *num_nodes = g->N;
   if (num_pieces) *num_pieces = g->P;
   if (device_bytes) *device_bytes = g->device_bytes;
+  return CKT_OK;
+}
+
+int ckt_graph_tile_info(const ckt_graph *g, int32_t *tiles, int64_t *steps,
+                        int64_t *stream_steps, uint32_t *error_word) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  if (tiles) *tiles = (int32_t)g->num_tiles;
+  if (steps) *steps = g->tile_num_steps;
+  if (stream_steps) *stream_steps = g->tile_stream_steps;
+  if (error_word) {
+    *error_word = 0;
+    if (g->tile_error)
+      CKT_CUDA(cudaMemcpy(error_word, g->tile_error, 4, cudaMemcpyDeviceToHost));
+  }
   return CKT_OK;
 }
 

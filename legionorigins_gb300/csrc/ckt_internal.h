@@ -57,6 +57,28 @@ constexpr uint32_t kPrivateBit = 0x80000000u;
 constexpr uint32_t kOffsetMask = 0x7fffffffu;
 constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 31 bits
 
+// Tiled distribute_charge (dc_tile_kernel).  Nodes are cut into tiles of at
+// most kTileNodesMax consecutive nodes, wires into chunks of kChunkWires.  A
+// tile's contributions are cut into steps, each covering an ascending range
+// of wires: a stream step is one chunk whose I[0]/I[9] slices the block
+// copies into shared memory whole; a gather step merges chunks with few of
+// the tile's contributions, whose currents are gathered one by one.  Steps
+// run in wire order and, inside a step, a node's contributions in wire
+// order, so every node still adds its contributions in the CSR's order.
+//   step record: {first entry, entries (padded to 4), chunk or kGatherStep,
+//                 first gather-wire slot}
+//   entry word: wire within chunk (11 bits) | end << 11 | node within tile
+//               << 12 (13 bits) | flush << 25 | head << 26 | private << 27
+// flush: the entry starts a new piece group and is not the node's first;
+// head: first entry of its node within the step.  Padding words are
+// kTePad (head set, skipped).
+constexpr uint32_t kTileNodesMax = 8192;
+constexpr uint32_t kChunkWires = 2048;
+constexpr uint32_t kGatherStep = 0xffffffffu;
+constexpr uint32_t kTeEnd = 1u << 11, kTeNodeShift = 12, kTeFlush = 1u << 25,
+                   kTeHead = 1u << 26, kTePriv = 1u << 27, kTePad = 0xffffffffu;
+constexpr uint32_t kStepEntriesMax = 2 * kChunkWires;  // padded entries of one step
+
 inline unsigned grid_for(uint64_t n, unsigned block = 256) {
   return (unsigned)((n + block - 1) / block);
 }
@@ -101,5 +123,14 @@ struct ckt_graph {
   uint32_t *slot_in = nullptr, *slot_out = nullptr;  // [W]
   uint32_t *gstart = nullptr;                        // [ceil(2W / 32)]
   float *contrib = nullptr;                          // [2W] scratch
+  // Tiled distribute_charge plan (see kTileNodesMax): tile t runs steps
+  // [tile_step[t], tile_step[t + 1]).
+  uint32_t tile_nodes = 0, num_tiles = 0;
+  int64_t tile_num_steps = 0, tile_stream_steps = 0;
+  uint32_t *tile_step = nullptr;   // [num_tiles + 1]
+  uint4 *tile_steps = nullptr;     // [steps]
+  uint32_t *tile_ent = nullptr;    // entry words, every step's run 16-byte aligned
+  uint32_t *tile_gw = nullptr;     // gather steps' wire indices, parallel to their entries
+  uint32_t *tile_error = nullptr;  // [1] bit 0: a copy wait timed out
   int64_t device_bytes = 0;
 };

@@ -3,6 +3,7 @@
 #include <climits>
 #include <cstring>
 
+#include "ckt_dctile.cuh"
 #include "ckt_internal.h"
 #include "ckt_kernels.cuh"
 
@@ -95,6 +96,55 @@ static int check_graph_wires(const ckt_graph *g, const ckt_wires &w) {
   CKT_REQUIRE(g != nullptr, "graph is NULL");
   CKT_REQUIRE(w.seg_stride >= g->W, "wires.seg_stride %lld is smaller than the graph's %lld wires",
               (long long)w.seg_stride, (long long)g->W);
+  return CKT_OK;
+}
+
+// The tiled node pass needs 16-byte aligned current slices that may be read
+// up to a multiple of 4 wires: current 16-byte aligned, seg_stride a
+// multiple of 4 (then seg_stride >= W rounds W up).
+static bool tile_plan_usable(const ckt_graph *g, const ckt_wires &w) {
+  return g->num_tiles > 0 && (reinterpret_cast<uintptr_t>(w.current) & 15u) == 0 &&
+         (w.seg_stride & 3) == 0;
+}
+
+// Bound of the tiled pass's copy waits; a wait that runs out sets the
+// graph's error word instead of hanging the block.
+constexpr uint64_t kTileTimeoutNs = 2000000000ull;
+
+template <bool UV>
+static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_nodes &n, float dt,
+                          cudaStream_t s) {
+  static thread_local int configured_device = -1;
+  int dev = 0;
+  CKT_CUDA(cudaGetDevice(&dev));
+  if (configured_device != dev) {
+    const int most = (int)dc_tile_smem_bytes(kTileNodesMax);
+    CKT_CUDA(cudaFuncSetAttribute(dc_tile_kernel<true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+    CKT_CUDA(cudaFuncSetAttribute(dc_tile_kernel<false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+    configured_device = dev;
+  }
+  DcTileArgs a;
+  a.tile_step = g->tile_step;
+  a.steps = g->tile_steps;
+  a.ent = g->tile_ent;
+  a.gw = g->tile_gw;
+  a.off = g->node_off;
+  a.I0 = w.current;
+  a.I9 = w.current + 9 * w.seg_stride;
+  a.charge = n.charge;
+  a.voltage = n.voltage;
+  a.cap = n.capacitance;
+  a.leak = n.leakage;
+  a.error = g->tile_error;
+  a.timeout_ns = kTileTimeoutNs;
+  a.N = (uint32_t)g->N;
+  a.W = (uint32_t)g->W;
+  a.tile_nodes = g->tile_nodes;
+  a.dt = dt;
+  dc_tile_kernel<UV><<<g->num_tiles, kTileBlock, dc_tile_smem_bytes(g->tile_nodes), s>>>(a);
+  CKT_CHECK_LAUNCH();
   return CKT_OK;
 }
 
@@ -207,6 +257,8 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   if (graph->N == 0 || graph->W == 0) return CKT_OK;  // no wire deposits anything
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
+  if (tile_plan_usable(graph, wires))
+    return launch_dc_tile<false>(graph, wires, nodes, prm->dt, as_stream(stream));
   // The staged gather: measured faster than scattering the contributions
   // into CSR order and summing them contiguously, whose random 4-byte writes
   // cost as much as the gathers they replace.
@@ -291,6 +343,8 @@ int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   if (graph->N == 0) return CKT_OK;
   if (graph->W == 0) return ckt_update_voltages_all(graph, nodes, stream);
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
+  if (tile_plan_usable(graph, wires))
+    return launch_dc_tile<true>(graph, wires, nodes, prm->dt, as_stream(stream));
   const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
   dcuv_kernel<<<grid_for(graph->N, kDcBlock), kDcBlock, 0, as_stream(stream)>>>(
       (uint32_t)graph->N, graph->node_off, graph->node_ent, I0, I9, nodes.charge, nodes.voltage,

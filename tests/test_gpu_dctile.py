@@ -1,0 +1,142 @@
+"""The tiled node pass (distribute_charge over node tiles, currents copied
+into shared memory in 2048-wire chunks) against the per-node gather form.
+
+The index-space distribute_charge and the fused node pass take the tiled
+form when the current array is 16-byte aligned and its segment stride is a
+multiple of 4, and the gather form otherwise.  Both must give the same bits
+as each other and as the oracle, on shapes with dense chunks, sparse
+(gathered) chunks, hub nodes whose runs cross many chunks, tiles that
+straddle pieces, and heavy cross-piece reduction.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import same_bits
+
+pytestmark = pytest.mark.gpu
+
+STATE = ["current", "voltage", "charge", "node_voltage"]
+FIELDS = ["in_ptr", "out_ptr", "in_loc", "out_loc", "L", "R", "C", "current", "voltage",
+          "charge", "node_voltage", "cap", "leak", "locator"]
+
+SHAPES = {
+    "cfg0": (4, 256, 1024, 95, 12345),
+    "heavy_reduction": (16, 64, 256, 50, 42),
+    "all_cross": (6, 16, 64, 0, 11),
+    "hub": (7, 3, 3000, 60, 8),
+    "many_pieces_per_tile": (40, 300, 1200, 95, 3),
+    "tile_per_piece": (3, 8192, 2048, 90, 5),
+    "tiles_straddle_pieces": (2, 20000, 80000, 97, 9),
+}
+
+
+class Strided:
+    """A device circuit whose current/voltage segments sit `stride` floats
+    apart (stride >= W); the gap holds NaN."""
+
+    def __init__(self, cuda, c, stride):
+        from legionorigins_gb300 import circuit as C
+
+        p = c.params
+        host = {k: np.ascontiguousarray(getattr(c, k)) for k in FIELDS}
+        self.dc = C.DeviceCircuit(host, C.Shape(p.num_pieces, p.nodes_per_piece,
+                                                p.wires_per_piece))
+        self.W, self.stride = self.dc.shape.W, stride
+        t = self.dc.t
+        for k, segs in (("current", 10), ("voltage", 9)):
+            buf = cuda.full((segs, stride), float("nan"), dtype=cuda.float32, device="cuda")
+            buf[:, :self.W] = t[k].view(segs, self.W)
+            t[k] = buf
+
+    def wires(self):
+        from legionorigins_gb300 import Wires
+
+        t = self.dc.t
+        return Wires(t["in_ptr"].data_ptr(), t["out_ptr"].data_ptr(), t["in_loc"].data_ptr(),
+                     t["out_loc"].data_ptr(), t["L"].data_ptr(), t["R"].data_ptr(),
+                     t["C"].data_ptr(), t["current"].data_ptr(), t["voltage"].data_ptr(),
+                     self.stride)
+
+    def loops(self, prm, n, fused):
+        from legionorigins_gb300 import check, lib
+
+        L, g, w, nd = lib(), self.dc.graph.handle, self.wires(), self.dc.nodes()
+        for _ in range(n):
+            check(L.ckt_calc_new_currents_all(g, w, nd, ctypes.byref(prm), None))
+            if fused:
+                check(L.ckt_distribute_update_all(g, w, nd, ctypes.byref(prm), None))
+            else:
+                check(L.ckt_distribute_charge_all(g, w, nd, ctypes.byref(prm), None))
+                check(L.ckt_update_voltages_all(g, nd, None))
+
+    def state(self, cuda):
+        cuda.cuda.synchronize()
+        t = self.dc.t
+        out = {k: t[k][:, :self.W].contiguous().cpu().numpy() for k in ("current", "voltage")}
+        out.update({k: t[k].cpu().numpy() for k in ("charge", "node_voltage")})
+        return out
+
+
+def tile_info(dc):
+    from legionorigins_gb300 import check, lib
+
+    tiles, steps, stream = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+    err = ctypes.c_uint32()
+    check(lib().ckt_graph_tile_info(dc.graph.handle, ctypes.byref(tiles), ctypes.byref(steps),
+                                    ctypes.byref(stream), ctypes.byref(err)))
+    return tiles.value, steps.value, stream.value, err.value
+
+
+@pytest.mark.parametrize("shape", sorted(SHAPES))
+@pytest.mark.parametrize("fused", [False, True], ids=["three_launch", "fused"])
+def test_tiled_equals_gather_and_oracle(cuda, oracle, shape, fused):
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(*SHAPES[shape], L_offset=0.001))
+    W = c.params.num_pieces * c.params.wires_per_piece
+    pad = (-W) % 4
+    tiled = Strided(cuda, c, W + pad + 4)   # a multiple of 4: the tiled form
+    gather = Strided(cuda, c, W + pad + 6)  # 2 mod 4: the gather form
+    prm = C.params(2, 0)
+    tiled.loops(prm, 3, fused)
+    gather.loops(prm, 3, fused)
+    a, b = tiled.state(cuda), gather.state(cuda)
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), (shape, k)
+    oracle.simulate(c, 3, 2)
+    for k in STATE:
+        assert same_bits(a[k], getattr(c, k)), (shape, k)
+    tiles, steps, stream, err = tile_info(tiled.dc)
+    assert tiles == -(-c.params.num_pieces * c.params.nodes_per_piece // 8192)
+    assert steps >= stream >= 0 and err == 0
+
+
+def test_plan_has_stream_and_gather_steps(cuda, oracle):
+    """Config-1 pieces (16384 nodes, 65536 wires each): each half-piece tile
+    copies its piece's 32 chunks and gathers its ghost contributions."""
+    c = oracle.generate(oracle.GenParams(4, 16384, 65536, 95, 12345, L_offset=0.001))
+    dc = Strided(cuda, c, 4 * 65536).dc
+    tiles, steps, stream, err = tile_info(dc)
+    assert tiles == 8
+    assert stream == 8 * 32
+    assert steps > stream
+    assert err == 0
+
+
+def test_nan_currents_propagate_identically(cuda, oracle):
+    """The divergent regime (S = 1000): NaN and +-Inf currents flow through
+    both forms to the same bits."""
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(*SHAPES["cfg0"], L_offset=0.001))
+    W = c.params.num_pieces * c.params.wires_per_piece
+    tiled, gather = Strided(cuda, c, W), Strided(cuda, c, W + 2)
+    prm = C.params(1000, 0)
+    tiled.loops(prm, 2, True)
+    gather.loops(prm, 2, True)
+    a, b = tiled.state(cuda), gather.state(cuda)
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    assert np.isnan(a["node_voltage"]).any()
