@@ -208,9 +208,9 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   }
   __syncthreads();
 
-  // Thread 0 issues the copies of stream step s into slot (s - s0) % stages.
-  auto issue = [&](uint32_t s) {
-    const uint4 st = a.steps[s];
+  // Thread 0 issues the copies of stream step s (record st) into slot
+  // (s - s0) % stages.
+  auto issue = [&](uint32_t s, const uint4 &st) {
     if (st.z == kGatherStep) return;
     const uint32_t slot = (s - s0) % kTileStages;
     const uint32_t w0 = st.z * kChunkWires;
@@ -223,12 +223,18 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     bulk_g2s(sent_of(slot), a.ent + st.x, st.y * 4, b);
   };
   if (threadIdx.x == 0)
-    for (uint32_t s = s0; s < min(s1, s0 + kTileStages); s++) issue(s);
+    for (uint32_t s = s0; s < min(s1, s0 + kTileStages); s++) issue(s, a.steps[s]);
 
+  // Step records are loaded one step ahead (and, by thread 0, the record of
+  // the step it issues next), so no global load latency sits between steps.
   uint32_t parity = 0;  // bit k: phase parity of slot k's next completion
   bool failed = false;
+  uint4 st_next = s0 < s1 ? a.steps[s0] : make_uint4(0u, 0u, 0u, 0u);
   for (uint32_t s = s0; s < s1; s++) {
-    const uint4 st = a.steps[s];
+    const uint4 st = st_next;
+    if (s + 1 < s1) st_next = a.steps[s + 1];
+    uint4 st_issue = make_uint4(0u, 0u, kGatherStep, 0u);
+    if (threadIdx.x == 0 && s + kTileStages < s1) st_issue = a.steps[s + kTileStages];
     const uint32_t slot = (s - s0) % kTileStages;
     const bool stream = st.z != kGatherStep;
     uint32_t *sent = sent_of(slot);
@@ -267,7 +273,7 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       failed = true;
       break;
     }
-    if (threadIdx.x == 0 && s + kTileStages < s1) issue(s + kTileStages);
+    if (threadIdx.x == 0 && s + kTileStages < s1) issue(s + kTileStages, st_issue);
   }
 
   if (failed) {

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cstring>
 #include <thread>
+#include <utility>
 
 #include "ckt_internal.h"
 
@@ -183,16 +184,28 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
            (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u);
   };
   // Emits [a, b) of `v` (sorted by node, then CSR position) as one step.
+  // A node's entries in the step form one run, summed by one thread; runs
+  // are laid out longest first so that the threads of a warp carry runs of
+  // about the same length.
+  std::vector<std::pair<uint32_t, uint32_t>> runs;  // (length, first index)
   auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
     const bool gather = chunk == kGatherStep;
     const uint32_t e0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
-    uint32_t prev = 0xffffffffu;
-    for (size_t j = a; j < b; j++) {
-      const uint32_t xl = (uint32_t)(v[j] >> 32) & (kTileNodesMax - 1);
-      tp.ent.push_back(word(v[j], xl != prev));
-      if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
-      prev = xl;
+    runs.clear();
+    for (size_t j = a; j < b;) {
+      const uint64_t node = v[j] >> 32;
+      size_t e = j + 1;
+      while (e < b && (v[e] >> 32) == node) e++;
+      runs.emplace_back((uint32_t)(e - j), (uint32_t)j);
+      j = e;
     }
+    std::stable_sort(runs.begin(), runs.end(),
+                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    for (const auto &r : runs)
+      for (uint32_t j = r.second; j < r.second + r.first; j++) {
+        tp.ent.push_back(word(v[j], j == r.second));
+        if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
+      }
     while (tp.ent.size() % 4) {  // 16-byte runs for the bulk copies
       tp.ent.push_back(kTePad);
       if (gather) tp.gw.push_back(0u);
