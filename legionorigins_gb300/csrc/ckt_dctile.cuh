@@ -87,7 +87,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 constexpr uint32_t kTileBlock = 1024;
-constexpr uint32_t kTileStages = 3;
+constexpr uint32_t kTileStages = 6;
 // Shared memory of one stage: I[0] and I[9] slices of a chunk, then the
 // step's entry words.
 constexpr uint32_t kStageVals = 2 * kChunkWires;

@@ -183,14 +183,15 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     return (w % kChunkWires) | ((u & 2u) ? kTeEnd : 0u) | (xl << kTeNodeShift) |
            (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u);
   };
-  // Emits [a, b) of `v` (sorted by node, then CSR position) as one step.
-  // A node's entries in the step form one run, summed by one thread; runs
-  // are laid out longest first so that the threads of a warp carry runs of
-  // about the same length.
+  // Emits [a, b) of `v` (sorted by node, then CSR position) as one step, or
+  // as several when it holds more entries than a step's buffer.  A node's
+  // entries in a step form one run, summed by one thread; runs are laid out
+  // longest first so that the threads of a warp carry runs of about the
+  // same length.  A run cut between two steps continues in the later one.
   std::vector<std::pair<uint32_t, uint32_t>> runs;  // (length, first index)
+  std::vector<uint32_t> order;
   auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
     const bool gather = chunk == kGatherStep;
-    const uint32_t e0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
     runs.clear();
     for (size_t j = a; j < b;) {
       const uint64_t node = v[j] >> 32;
@@ -201,25 +202,32 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     }
     std::stable_sort(runs.begin(), runs.end(),
                      [](const auto &x, const auto &y) { return x.first > y.first; });
+    order.clear();
     for (const auto &r : runs)
-      for (uint32_t j = r.second; j < r.second + r.first; j++) {
-        tp.ent.push_back(word(v[j], j == r.second));
+      for (uint32_t j = r.second; j < r.second + r.first; j++) order.push_back(j);
+    constexpr size_t kMax = kStepEntriesMax - 4;
+    for (size_t c0 = 0; c0 < order.size(); c0 += kMax) {
+      const size_t c1 = std::min(order.size(), c0 + kMax);
+      const uint32_t e0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
+      for (size_t q = c0; q < c1; q++) {
+        const uint32_t j = order[q];
+        const bool head = q == c0 || (v[order[q - 1]] >> 32) != (v[j] >> 32);
+        tp.ent.push_back(word(v[j], head));
         if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
       }
-    while (tp.ent.size() % 4) {  // 16-byte runs for the bulk copies
-      tp.ent.push_back(kTePad);
-      if (gather) tp.gw.push_back(0u);
+      while (tp.ent.size() % 4) {  // 16-byte runs for the bulk copies
+        tp.ent.push_back(kTePad);
+        if (gather) tp.gw.push_back(0u);
+      }
+      tp.steps.push_back(make_uint4(e0, (uint32_t)tp.ent.size() - e0, chunk, g0));
     }
-    tp.steps.push_back(make_uint4(e0, (uint32_t)tp.ent.size() - e0, chunk, g0));
   };
   auto flush_sparse = [&]() {
     if (sparse.empty()) return;
     // One wire range: order by (node, CSR position) only.
     for (uint64_t &k : sparse) k &= (1ull << 45) - 1;
     std::sort(sparse.begin(), sparse.end());
-    constexpr size_t kMax = kStepEntriesMax - 4;
-    for (size_t a = 0; a < sparse.size(); a += kMax)
-      emit(sparse, a, std::min(sparse.size(), a + kMax), kGatherStep);
+    emit(sparse, 0, sparse.size(), kGatherStep);
     sparse.clear();
   };
   sparse.clear();

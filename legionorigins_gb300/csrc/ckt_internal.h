@@ -60,11 +60,12 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 // Tiled distribute_charge (dc_tile_kernel).  Nodes are cut into tiles of at
 // most kTileNodesMax consecutive nodes, wires into chunks of kChunkWires.  A
 // tile's contributions are cut into steps, each covering an ascending range
-// of wires: a stream step is one chunk whose I[0]/I[9] slices the block
-// copies into shared memory whole; a gather step merges chunks with few of
-// the tile's contributions, whose currents are gathered one by one.  Steps
-// run in wire order and, inside a step, a node's contributions in wire
-// order, so every node still adds its contributions in the CSR's order.
+// of wires: a stream step holds entries of one chunk, whose I[0]/I[9] slices
+// the block copies into shared memory whole (a chunk with more entries than
+// a step holds takes consecutive steps); a gather step merges chunks with
+// few of the tile's contributions, whose currents are gathered one by one.
+// Steps run in wire order and, inside a step, a node's contributions in
+// wire order, so every node still adds its contributions in the CSR's order.
 //   step record: {first entry, entries (padded to 4), chunk or kGatherStep,
 //                 first gather-wire slot}
 //   entry word: wire within chunk (11 bits) | end << 11 | node within tile
@@ -77,7 +78,7 @@ constexpr uint32_t kChunkWires = 2048;
 constexpr uint32_t kGatherStep = 0xffffffffu;
 constexpr uint32_t kTeEnd = 1u << 11, kTeNodeShift = 12, kTeFlush = 1u << 25,
                    kTeHead = 1u << 26, kTePriv = 1u << 27, kTePad = 0xffffffffu;
-constexpr uint32_t kStepEntriesMax = 2 * kChunkWires;  // padded entries of one step
+constexpr uint32_t kStepEntriesMax = kChunkWires;  // padded entries of one step
 
 inline unsigned grid_for(uint64_t n, unsigned block = 256) {
   return (unsigned)((n + block - 1) / block);

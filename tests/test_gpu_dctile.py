@@ -115,12 +115,13 @@ def test_tiled_equals_gather_and_oracle(cuda, oracle, shape, fused):
 
 def test_plan_has_stream_and_gather_steps(cuda, oracle):
     """Config-1 pieces (16384 nodes, 65536 wires each): each half-piece tile
-    copies its piece's 32 chunks and gathers its ghost contributions."""
+    copies its piece's 32 chunks (a chunk with more of the tile's entries
+    than a step holds takes two steps) and gathers its ghost contributions."""
     c = oracle.generate(oracle.GenParams(4, 16384, 65536, 95, 12345, L_offset=0.001))
     dc = Strided(cuda, c, 4 * 65536).dc
     tiles, steps, stream, err = tile_info(dc)
     assert tiles == 8
-    assert stream == 8 * 32
+    assert 8 * 32 <= stream <= 8 * 64
     assert steps > stream
     assert err == 0
 
