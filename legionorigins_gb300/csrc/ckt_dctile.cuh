@@ -86,12 +86,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   }
 }
 
-constexpr uint32_t kTileBlock = 1024;
+constexpr uint32_t kTileBlock = 32 * (kTileWarps + 1);  // consumer warps + one copy warp
 constexpr uint32_t kTileStages = 6;
-// Shared memory of one stage: I[0] and I[9] slices of a chunk, then the
-// step's entry words.
+// Shared memory of one stage: I[0] and I[9] slices of a chunk (a gather
+// step's wire indices instead), then the step's block (header + entries).
 constexpr uint32_t kStageVals = 2 * kChunkWires;
-constexpr uint32_t kStageBytes = (kStageVals + kStepEntriesMax) * 4;
+constexpr uint32_t kStageBlockWords = kStepHeaderWords + kStepEntriesMax;
+constexpr uint32_t kStageBytes = (kStageVals + kStageBlockWords) * 4;
 
 struct DcTileArgs {
   const uint32_t *tile_step;
@@ -108,28 +109,47 @@ struct DcTileArgs {
 };
 
 __host__ __device__ constexpr uint32_t dc_tile_smem_bytes(uint32_t tile_nodes) {
-  return 2 * tile_nodes * 4 + kTileStages * kStageBytes + kTileStages * 8;
+  return 2 * tile_nodes * 4 + kTileStages * kStageBytes + 2 * kTileStages * 8 + 16;
 }
 
-// Block-wide: sums the step's node runs.  Entries and stream values are in
-// shared memory; for a gather step value k is sval[k].  Each thread takes
-// kWalkRows entries per pass; a row whose entry heads a run carries that
-// run to its end, one entry per round, so the rows' shared-memory loads
-// overlap instead of forming one dependent chain per thread.
-constexpr uint32_t kWalkRows = 2;
+// Bounded wait that also gives up once another thread has raised `abort`.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar, uint32_t parity,
+                                                    const volatile uint32_t *abort,
+                                                    uint64_t timeout_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = dct_now_ns();
+  for (;;) {
+    for (int k = 0; k < 16; k++)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (*abort != 0u || dct_now_ns() - t0 > timeout_ns) return false;
+  }
+}
 
-__device__ __forceinline__ void dc_tile_walk(const uint32_t *sent, const float *sval,
-                                             uint32_t cnt, bool stream, float *sacc,
-                                             float *sfold, float dt) {
-  for (uint32_t j0 = 0; j0 < cnt; j0 += kWalkRows * kTileBlock) {
-    uint32_t u[kWalkRows], k[kWalkRows], node[kWalkRows];
-    float acc[kWalkRows], fold[kWalkRows];
-    bool head[kWalkRows], live[kWalkRows];
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// One warp sums its node runs of a step: entries [b, e) of the step's block.
+// Stream steps read currents from the staged chunk slices, gather steps from
+// global memory through the staged wire indices.  Each lane takes two
+// entries per pass; a lane whose entry heads a run carries the run to its
+// end, one entry per round, so the two rows' loads overlap.
+__device__ __forceinline__ void dc_tile_warp_walk(const uint32_t *sent, const float *svals,
+                                                  uint32_t b, uint32_t e, bool stream,
+                                                  const float *__restrict__ I0,
+                                                  const float *__restrict__ I9, float *sacc,
+                                                  float *sfold, float dt, uint32_t lane) {
+  const uint32_t *sgw = reinterpret_cast<const uint32_t *>(svals);
+  constexpr uint32_t kRows = 2;
+  for (uint32_t j0 = b; j0 < e; j0 += kRows * 32) {
+    uint32_t u[kRows], k[kRows], node[kRows];
+    float acc[kRows], fold[kRows];
+    bool head[kRows], live[kRows];
     bool any = false;
 #pragma unroll
-    for (uint32_t r = 0; r < kWalkRows; r++) {
-      k[r] = j0 + r * kTileBlock + threadIdx.x;
-      u[r] = k[r] < cnt ? sent[k[r]] : kTePad;
+    for (uint32_t r = 0; r < kRows; r++) {
+      k[r] = j0 + r * 32 + lane;
+      u[r] = k[r] < e ? sent[k[r]] : kTePad;
       head[r] = (u[r] & kTeHead) && u[r] != kTePad;
       live[r] = head[r];
       node[r] = (u[r] >> kTeNodeShift) & (kTileNodesMax - 1);
@@ -144,11 +164,16 @@ __device__ __forceinline__ void dc_tile_walk(const uint32_t *sent, const float *
     while (any) {
       any = false;
 #pragma unroll
-      for (uint32_t r = 0; r < kWalkRows; r++) {
+      for (uint32_t r = 0; r < kRows; r++) {
         if (!live[r]) continue;
         const uint32_t end = (u[r] >> 11) & 1u;
-        const float v =
-            stream ? sval[end * kChunkWires + (u[r] & (kChunkWires - 1))] : sval[k[r]];
+        float v;
+        if (stream) {
+          v = svals[end * kChunkWires + (u[r] & (kChunkWires - 1))];
+        } else {
+          const uint32_t w = sgw[k[r]];
+          v = end ? I9[w] : I0[w];
+        }
         const float c = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
         if (u[r] & kTePriv) {
           acc[r] = __fadd_rn(acc[r], c);
@@ -159,7 +184,7 @@ __device__ __forceinline__ void dc_tile_walk(const uint32_t *sent, const float *
           }
           fold[r] = __fadd_rn(fold[r], c);
         }
-        if (++k[r] < cnt) {
+        if (++k[r] < e) {
           u[r] = sent[k[r]];
           live[r] = !(u[r] & kTeHead);  // the next node's run, or padding
         } else {
@@ -169,7 +194,7 @@ __device__ __forceinline__ void dc_tile_walk(const uint32_t *sent, const float *
       }
     }
 #pragma unroll
-    for (uint32_t r = 0; r < kWalkRows; r++)
+    for (uint32_t r = 0; r < kRows; r++)
       if (head[r]) {
         sacc[node[r]] = acc[r];
         sfold[node[r]] = fold[r];
@@ -177,8 +202,13 @@ __device__ __forceinline__ void dc_tile_walk(const uint32_t *sent, const float *
   }
 }
 
-// One block per node tile.  UV = true also applies update_voltages to the
-// tile's nodes (the fused node pass: charge ends at zero).
+// One block per node tile: warp kTileWarps (lane 0) copies the steps' data
+// into a ring of kTileStages stages; consumer warp w sums the runs of the
+// tile's nodes n with n mod kTileWarps == w, so no two warps touch a node
+// and the warps run through the steps independently, each handing its stage
+// back through the stage's `empty` barrier.  UV = true also applies
+// update_voltages to the tile's nodes (the fused node pass: charge ends at
+// zero).
 template <bool UV>
 __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   extern __shared__ __align__(128) unsigned char dct_smem[];
@@ -186,20 +216,27 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   float *sacc = reinterpret_cast<float *>(dct_smem);
   float *sfold = sacc + TN;
   unsigned char *stage0 = dct_smem + 2 * TN * 4;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(stage0 + kTileStages * kStageBytes);
-  auto sval_of = [&](uint32_t slot) {
+  uint64_t *full = reinterpret_cast<uint64_t *>(stage0 + kTileStages * kStageBytes);
+  uint64_t *empty = full + kTileStages;
+  volatile uint32_t *abort = reinterpret_cast<volatile uint32_t *>(empty + kTileStages);
+  auto vals_of = [&](uint32_t slot) {
     return reinterpret_cast<float *>(stage0 + slot * kStageBytes);
   };
-  auto sent_of = [&](uint32_t slot) {
+  auto block_of = [&](uint32_t slot) {
     return reinterpret_cast<uint32_t *>(stage0 + slot * kStageBytes + kStageVals * 4);
   };
 
   const uint32_t t = blockIdx.x;
   const uint32_t x0 = t * TN, xe = min(a.N, x0 + TN), nn = xe - x0;
   const uint32_t s0 = a.tile_step[t], s1 = a.tile_step[t + 1];
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
 
   if (threadIdx.x == 0) {
-    for (uint32_t k = 0; k < kTileStages; k++) mbar_init(bar + k, 1);
+    for (uint32_t k = 0; k < kTileStages; k++) {
+      mbar_init(full + k, 1);
+      mbar_init(empty + k, kTileWarps);
+    }
+    *abort = 0u;
     mbar_init_fence();
   }
   for (uint32_t i = threadIdx.x; i < nn; i += kTileBlock) {
@@ -208,81 +245,66 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   }
   __syncthreads();
 
-  // Thread 0 issues the copies of stream step s (record st) into slot
-  // (s - s0) % stages.
-  auto issue = [&](uint32_t s, const uint4 &st) {
-    if (st.z == kGatherStep) return;
-    const uint32_t slot = (s - s0) % kTileStages;
-    const uint32_t w0 = st.z * kChunkWires;
-    const uint32_t nw = (min(kChunkWires, a.W - w0) + 3u) & ~3u;
-    uint64_t *b = bar + slot;
-    fence_proxy_async_smem();
-    mbar_expect_tx(b, 2 * nw * 4 + st.y * 4);
-    bulk_g2s(sval_of(slot), a.I0 + w0, nw * 4, b);
-    bulk_g2s(sval_of(slot) + kChunkWires, a.I9 + w0, nw * 4, b);
-    bulk_g2s(sent_of(slot), a.ent + st.x, st.y * 4, b);
-  };
-  if (threadIdx.x == 0)
-    for (uint32_t s = s0; s < min(s1, s0 + kTileStages); s++) issue(s, a.steps[s]);
-
-  // Step records are loaded one step ahead (and, by thread 0, the record of
-  // the step it issues next), so no global load latency sits between steps.
-  uint32_t parity = 0;  // bit k: phase parity of slot k's next completion
-  bool failed = false;
-  uint4 st_next = s0 < s1 ? a.steps[s0] : make_uint4(0u, 0u, 0u, 0u);
-  for (uint32_t s = s0; s < s1; s++) {
-    const uint4 st = st_next;
-    if (s + 1 < s1) st_next = a.steps[s + 1];
-    uint4 st_issue = make_uint4(0u, 0u, kGatherStep, 0u);
-    if (threadIdx.x == 0 && s + kTileStages < s1) st_issue = a.steps[s + kTileStages];
-    const uint32_t slot = (s - s0) % kTileStages;
-    const bool stream = st.z != kGatherStep;
-    uint32_t *sent = sent_of(slot);
-    float *sval = sval_of(slot);
-    bool ok = true;
-    if (stream) {
-      ok = mbar_wait_bounded(bar + slot, (parity >> slot) & 1u, a.timeout_ns);
-      if (ok) parity ^= 1u << slot;
-    } else {
-      // Gather step: entry words and currents staged by all threads, with
-      // several independent loads in flight per thread.
-      constexpr uint32_t kBatch = kStepEntriesMax / kTileBlock;
-      for (uint32_t j0 = 0; j0 < st.y; j0 += kBatch * kTileBlock) {
-        uint32_t u[kBatch], w[kBatch];
-#pragma unroll
-        for (uint32_t r = 0; r < kBatch; r++) {
-          const uint32_t j = j0 + r * kTileBlock + threadIdx.x;
-          u[r] = j < st.y ? a.ent[st.x + j] : kTePad;
-          w[r] = j < st.y ? a.gw[st.w + j] : 0u;
+  uint32_t issued = 0;  // copy warp: steps issued
+  if (warp == kTileWarps) {
+    if (lane == 0) {
+      for (uint32_t s = s0; s < s1; s++) {
+        const uint32_t n = s - s0, slot = n % kTileStages;
+        if (n >= kTileStages &&
+            !mbar_wait_abortable(empty + slot, ((n / kTileStages) - 1) & 1u, abort,
+                                 a.timeout_ns)) {
+          *abort = 1u;
+          break;
         }
-#pragma unroll
-        for (uint32_t r = 0; r < kBatch; r++) {
-          const uint32_t j = j0 + r * kTileBlock + threadIdx.x;
-          if (j < st.y) {
-            float v = 0.0f;
-            if (u[r] != kTePad) v = (u[r] & kTeEnd) ? a.I9[w[r]] : a.I0[w[r]];
-            sent[j] = u[r];
-            sval[j] = v;
-          }
+        const uint4 st = a.steps[s];
+        const uint32_t nent = st.y - kStepHeaderWords;
+        uint32_t bytes = st.y * 4, nw = 0;
+        if (st.z != kGatherStep) {
+          nw = (min(kChunkWires, a.W - st.z * kChunkWires) + 3u) & ~3u;
+          bytes += 2 * nw * 4;
+        } else {
+          bytes += nent * 4;
         }
+        uint64_t *bar = full + slot;
+        fence_proxy_async_smem();
+        mbar_expect_tx(bar, bytes);
+        if (st.z != kGatherStep) {
+          bulk_g2s(vals_of(slot), a.I0 + st.z * kChunkWires, nw * 4, bar);
+          bulk_g2s(vals_of(slot) + kChunkWires, a.I9 + st.z * kChunkWires, nw * 4, bar);
+        } else if (nent > 0) {
+          bulk_g2s(vals_of(slot), a.gw + st.w, nent * 4, bar);
+        }
+        bulk_g2s(block_of(slot), a.ent + st.x, st.y * 4, bar);
+        issued = n + 1;
       }
-      __syncthreads();
     }
-    if (ok) dc_tile_walk(sent, sval, st.y, stream, sacc, sfold, a.dt);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
+  } else {
+    for (uint32_t s = s0; s < s1; s++) {
+      const uint32_t n = s - s0, slot = n % kTileStages;
+      if (!mbar_wait_abortable(full + slot, (n / kTileStages) & 1u, abort, a.timeout_ns)) {
+        *abort = 1u;
+        break;
+      }
+      const uint32_t *blk = block_of(slot);
+      const uint16_t *hdr = reinterpret_cast<const uint16_t *>(blk);
+      const uint32_t last = hdr[2 * kStepHeaderWords - 1];
+      const uint32_t total = last & ~kStepGatherFlag;
+      const uint32_t b = hdr[warp], e = warp + 1 < kTileWarps ? hdr[warp + 1] : total;
+      dc_tile_warp_walk(blk + kStepHeaderWords, vals_of(slot), b, e,
+                        (last & kStepGatherFlag) == 0u, a.I0, a.I9, sacc, sfold, a.dt, lane);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty + slot);
     }
-    if (threadIdx.x == 0 && s + kTileStages < s1) issue(s + kTileStages, st_issue);
   }
+  __syncthreads();
 
-  if (failed) {
-    // A copy never completed: report it, let the copies still in flight
-    // land (bounded), and leave the tile's charges unwritten.
-    if (threadIdx.x == 0) {
+  if (*abort != 0u) {
+    // A wait ran out: report it, let the copies still in flight land
+    // (bounded), and leave the tile's charges unwritten.
+    if (warp == kTileWarps && lane == 0) {
       atomicOr(a.error, 1u);
-      for (uint32_t k = 0; k < kTileStages; k++)
-        mbar_wait_bounded(bar + k, (parity >> k) & 1u, a.timeout_ns);
+      for (uint32_t n = issued > kTileStages ? issued - kTileStages : 0; n < issued; n++)
+        mbar_wait_bounded(full + n % kTileStages, (n / kTileStages) & 1u, a.timeout_ns);
     }
     return;
   }

@@ -185,11 +185,12 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
   };
   // Emits [a, b) of `v` (sorted by node, then CSR position) as one step, or
   // as several when it holds more entries than a step's buffer.  A node's
-  // entries in a step form one run, summed by one thread; runs are laid out
-  // longest first so that the threads of a warp carry runs of about the
-  // same length.  A run cut between two steps continues in the later one.
+  // entries in a step form one run, summed by one thread of the warp that
+  // owns the node; each warp's runs are laid out longest first so that its
+  // threads carry runs of about the same length.  A run cut between two
+  // steps continues in the later one.
   std::vector<std::pair<uint32_t, uint32_t>> runs;  // (length, first index)
-  std::vector<uint32_t> order;
+  std::vector<uint32_t> order, byw;
   auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
     const bool gather = chunk == kGatherStep;
     runs.clear();
@@ -208,18 +209,37 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     constexpr size_t kMax = kStepEntriesMax - 4;
     for (size_t c0 = 0; c0 < order.size(); c0 += kMax) {
       const size_t c1 = std::min(order.size(), c0 + kMax);
-      const uint32_t e0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
-      for (size_t q = c0; q < c1; q++) {
-        const uint32_t j = order[q];
-        const bool head = q == c0 || (v[order[q - 1]] >> 32) != (v[j] >> 32);
+      // Group the step's entries by owning warp, keeping their order.
+      uint32_t start[kTileWarps + 1] = {};
+      for (size_t q = c0; q < c1; q++)
+        start[((uint32_t)(v[order[q]] >> 32) & (kTileNodesMax - 1)) % kTileWarps + 1]++;
+      for (uint32_t w = 0; w < kTileWarps; w++) start[w + 1] += start[w];
+      byw.assign(c1 - c0, 0u);
+      uint32_t fill[kTileWarps];
+      for (uint32_t w = 0; w < kTileWarps; w++) fill[w] = start[w];
+      for (size_t q = c0; q < c1; q++)
+        byw[fill[((uint32_t)(v[order[q]] >> 32) & (kTileNodesMax - 1)) % kTileWarps]++] =
+            order[q];
+      const uint32_t n = (uint32_t)(c1 - c0);
+      const uint32_t b0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
+      uint16_t hdr[2 * kStepHeaderWords];
+      for (uint32_t w = 0; w < kTileWarps; w++) hdr[w] = (uint16_t)start[w];
+      hdr[2 * kStepHeaderWords - 1] = (uint16_t)(n | (gather ? kStepGatherFlag : 0u));
+      for (uint32_t h = 0; h < kStepHeaderWords; h++)
+        tp.ent.push_back((uint32_t)hdr[2 * h] | ((uint32_t)hdr[2 * h + 1] << 16));
+      uint32_t w = 0;
+      for (uint32_t q = 0; q < n; q++) {
+        while (q >= start[w + 1]) w++;
+        const uint32_t j = byw[q];
+        const bool head = q == start[w] || (v[byw[q - 1]] >> 32) != (v[j] >> 32);
         tp.ent.push_back(word(v[j], head));
         if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
       }
-      while (tp.ent.size() % 4) {  // 16-byte runs for the bulk copies
+      while ((tp.ent.size() - b0) % 4) {  // 16-byte blocks for the bulk copies
         tp.ent.push_back(kTePad);
         if (gather) tp.gw.push_back(0u);
       }
-      tp.steps.push_back(make_uint4(e0, (uint32_t)tp.ent.size() - e0, chunk, g0));
+      tp.steps.push_back(make_uint4(b0, (uint32_t)tp.ent.size() - b0, chunk, g0));
     }
   };
   auto flush_sparse = [&]() {
