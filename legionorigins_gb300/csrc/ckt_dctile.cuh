@@ -129,76 +129,60 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// One warp sums its node runs of a step: entries [b, e) of the step's block.
-// Stream steps read currents from the staged chunk slices, gather steps from
-// global memory through the staged wire indices.  Each lane takes two
-// entries per pass; a lane whose entry heads a run carries the run to its
-// end, one entry per round, so the two rows' loads overlap.
+// One warp sums its node runs of a step: entries [b, e) of the step's block,
+// stored 32 runs at a time, round by round (the plan's layout): in a round,
+// lane L takes the next entry of its run at position q + L, and the lanes
+// whose runs continue are a prefix of the warp, counted by a ballot.  Stream
+// steps read currents from the staged chunk slices, gather steps from global
+// memory through the staged wire indices.
 __device__ __forceinline__ void dc_tile_warp_walk(const uint32_t *sent, const float *svals,
                                                   uint32_t b, uint32_t e, bool stream,
                                                   const float *__restrict__ I0,
                                                   const float *__restrict__ I9, float *sacc,
                                                   float *sfold, float dt, uint32_t lane) {
   const uint32_t *sgw = reinterpret_cast<const uint32_t *>(svals);
-  constexpr uint32_t kRows = 2;
-  for (uint32_t j0 = b; j0 < e; j0 += kRows * 32) {
-    uint32_t u[kRows], k[kRows], node[kRows];
-    float acc[kRows], fold[kRows];
-    bool head[kRows], live[kRows];
-    bool any = false;
-#pragma unroll
-    for (uint32_t r = 0; r < kRows; r++) {
-      k[r] = j0 + r * 32 + lane;
-      u[r] = k[r] < e ? sent[k[r]] : kTePad;
-      head[r] = (u[r] & kTeHead) && u[r] != kTePad;
-      live[r] = head[r];
-      node[r] = (u[r] >> kTeNodeShift) & (kTileNodesMax - 1);
-      acc[r] = 0.0f;
-      fold[r] = 0.0f;
-      if (head[r]) {
-        acc[r] = sacc[node[r]];
-        fold[r] = sfold[node[r]];
-      }
-      any |= head[r];
+  uint32_t p = b;
+  while (p < e) {
+    uint32_t u = p + lane < e ? sent[p + lane] : 0u;
+    const bool first = (u & kTeHead) != 0u && u != kTePad;
+    const uint32_t node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
+    float acc = 0.0f, fold = 0.0f;
+    if (first) {
+      acc = sacc[node];
+      fold = sfold[node];
     }
-    while (any) {
-      any = false;
-#pragma unroll
-      for (uint32_t r = 0; r < kRows; r++) {
-        if (!live[r]) continue;
-        const uint32_t end = (u[r] >> 11) & 1u;
+    bool mine = first;
+    uint32_t c = __popc(__ballot_sync(0xffffffffu, mine));
+    while (c != 0u) {
+      if (mine) {
+        const uint32_t end = (u >> 11) & 1u;
         float v;
         if (stream) {
-          v = svals[end * kChunkWires + (u[r] & (kChunkWires - 1))];
+          v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
         } else {
-          const uint32_t w = sgw[k[r]];
+          const uint32_t w = sgw[p + lane];
           v = end ? I9[w] : I0[w];
         }
-        const float c = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
-        if (u[r] & kTePriv) {
-          acc[r] = __fadd_rn(acc[r], c);
+        const float cv = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
+        if (u & kTePriv) {
+          acc = __fadd_rn(acc, cv);
         } else {
-          if (u[r] & kTeFlush) {
-            acc[r] = __fadd_rn(acc[r], fold[r]);
-            fold[r] = 0.0f;
+          if (u & kTeFlush) {
+            acc = __fadd_rn(acc, fold);
+            fold = 0.0f;
           }
-          fold[r] = __fadd_rn(fold[r], c);
+          fold = __fadd_rn(fold, cv);
         }
-        if (++k[r] < e) {
-          u[r] = sent[k[r]];
-          live[r] = !(u[r] & kTeHead);  // the next node's run, or padding
-        } else {
-          live[r] = false;
-        }
-        any |= live[r];
       }
+      p += c;
+      mine = mine && (u & kTeCont) != 0u;
+      c = __popc(__ballot_sync(0xffffffffu, mine));
+      if (mine) u = sent[p + lane];
     }
-#pragma unroll
-    for (uint32_t r = 0; r < kRows; r++)
-      if (head[r]) {
-        sacc[node[r]] = acc[r];
-        sfold[node[r]] = fold[r];
-      }
+    if (first) {
+      sacc[node] = acc;
+      sfold[node] = fold;
+    }
   }
 }
 

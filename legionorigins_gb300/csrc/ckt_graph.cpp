@@ -174,23 +174,27 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
   }
   std::sort(keys.begin(), keys.end());
 
-  auto word = [&](uint64_t key, bool head) -> uint32_t {
+  auto word = [&](uint64_t key, bool head, bool cont) -> uint32_t {
     const uint32_t xl = (uint32_t)(key >> 32) & (kTileNodesMax - 1);
     const uint32_t i = lo + (uint32_t)key, x = x0 + xl;
     const uint32_t u = ent[i], w = u >> 2;
     const bool priv = (off[x] & kPrivateBit) != 0;
     const bool flush = !priv && (u & 1u) && i != (off[x] & kOffsetMask);
     return (w % kChunkWires) | ((u & 2u) ? kTeEnd : 0u) | (xl << kTeNodeShift) |
-           (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u);
+           (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u) |
+           (cont ? kTeCont : 0u);
   };
   // Emits [a, b) of `v` (sorted by node, then CSR position) as one step, or
-  // as several when it holds more entries than a step's buffer.  A node's
-  // entries in a step form one run, summed by one thread of the warp that
-  // owns the node; each warp's runs are laid out longest first so that its
-  // threads carry runs of about the same length.  A run cut between two
-  // steps continues in the later one.
+  // as several when it holds more entries than a step's buffer (a node's
+  // entries cut between two steps continue in the later one).  Inside a
+  // step, a node's entries form one run, summed by one lane of the warp that
+  // owns the node.  Each warp's runs are taken longest first, 32 at a time
+  // (one per lane), and stored round by round: the first entries of the 32
+  // runs, then the second entries of the runs that have one, and so on, so
+  // that in every round the lanes still busy are a prefix of the warp.
   std::vector<std::pair<uint32_t, uint32_t>> runs;  // (length, first index)
-  std::vector<uint32_t> order, byw;
+  std::vector<uint32_t> order;
+  std::vector<std::pair<uint32_t, uint32_t>> wruns[kTileWarps];
   auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
     const bool gather = chunk == kGatherStep;
     runs.clear();
@@ -206,35 +210,41 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     order.clear();
     for (const auto &r : runs)
       for (uint32_t j = r.second; j < r.second + r.first; j++) order.push_back(j);
+    auto node_of = [&](uint32_t j) { return (uint32_t)(v[j] >> 32) & (kTileNodesMax - 1); };
     constexpr size_t kMax = kStepEntriesMax - 4;
     for (size_t c0 = 0; c0 < order.size(); c0 += kMax) {
       const size_t c1 = std::min(order.size(), c0 + kMax);
-      // Group the step's entries by owning warp, keeping their order.
-      uint32_t start[kTileWarps + 1] = {};
-      for (size_t q = c0; q < c1; q++)
-        start[((uint32_t)(v[order[q]] >> 32) & (kTileNodesMax - 1)) % kTileWarps + 1]++;
-      for (uint32_t w = 0; w < kTileWarps; w++) start[w + 1] += start[w];
-      byw.assign(c1 - c0, 0u);
-      uint32_t fill[kTileWarps];
-      for (uint32_t w = 0; w < kTileWarps; w++) fill[w] = start[w];
-      for (size_t q = c0; q < c1; q++)
-        byw[fill[((uint32_t)(v[order[q]] >> 32) & (kTileNodesMax - 1)) % kTileWarps]++] =
-            order[q];
-      const uint32_t n = (uint32_t)(c1 - c0);
+      // The step's runs (pieces of `order` with one node), by owning warp.
+      for (auto &wr : wruns) wr.clear();
+      for (size_t q = c0; q < c1;) {
+        size_t e = q + 1;
+        while (e < c1 && node_of(order[e]) == node_of(order[q])) e++;
+        wruns[node_of(order[q]) % kTileWarps].emplace_back((uint32_t)(e - q), (uint32_t)q);
+        q = e;
+      }
       const uint32_t b0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
-      uint16_t hdr[2 * kStepHeaderWords];
-      for (uint32_t w = 0; w < kTileWarps; w++) hdr[w] = (uint16_t)start[w];
+      for (uint32_t h = 0; h < kStepHeaderWords; h++) tp.ent.push_back(0u);
+      uint16_t hdr[2 * kStepHeaderWords] = {};
+      uint32_t n = 0;
+      for (uint32_t w = 0; w < kTileWarps; w++) {
+        hdr[w] = (uint16_t)n;
+        auto &wr = wruns[w];
+        std::stable_sort(wr.begin(), wr.end(),
+                         [](const auto &x, const auto &y) { return x.first > y.first; });
+        for (size_t p0 = 0; p0 < wr.size(); p0 += 32) {
+          const size_t p1 = std::min(wr.size(), p0 + 32);
+          for (uint32_t r = 0; r < wr[p0].first; r++)
+            for (size_t k = p0; k < p1 && wr[k].first > r; k++) {
+              const uint32_t j = order[wr[k].second + r];
+              tp.ent.push_back(word(v[j], r == 0, r + 1 < wr[k].first));
+              if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
+              n++;
+            }
+        }
+      }
       hdr[2 * kStepHeaderWords - 1] = (uint16_t)(n | (gather ? kStepGatherFlag : 0u));
       for (uint32_t h = 0; h < kStepHeaderWords; h++)
-        tp.ent.push_back((uint32_t)hdr[2 * h] | ((uint32_t)hdr[2 * h + 1] << 16));
-      uint32_t w = 0;
-      for (uint32_t q = 0; q < n; q++) {
-        while (q >= start[w + 1]) w++;
-        const uint32_t j = byw[q];
-        const bool head = q == start[w] || (v[byw[q - 1]] >> 32) != (v[j] >> 32);
-        tp.ent.push_back(word(v[j], head));
-        if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
-      }
+        tp.ent[b0 + h] = (uint32_t)hdr[2 * h] | ((uint32_t)hdr[2 * h + 1] << 16);
       while ((tp.ent.size() - b0) % 4) {  // 16-byte blocks for the bulk copies
         tp.ent.push_back(kTePad);
         if (gather) tp.gw.push_back(0u);

@@ -75,14 +75,16 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 //                 first gather-wire slot (parallel to the entries)}
 //   entry word: wire within chunk (11 bits) | end << 11 | node within tile
 //               << 12 (13 bits) | flush << 25 | head << 26 | private << 27
+//               | continues << 28
 // flush: the entry starts a new piece group and is not the node's first;
-// head: first entry of its node within the step.  Padding words are
-// kTePad (head set, skipped).
+// head: first entry of its node within the step; continues: the node has
+// another entry in the step.  Padding words are kTePad.
 constexpr uint32_t kTileNodesMax = 8192;
 constexpr uint32_t kChunkWires = 2048;
 constexpr uint32_t kGatherStep = 0xffffffffu;
 constexpr uint32_t kTeEnd = 1u << 11, kTeNodeShift = 12, kTeFlush = 1u << 25,
-                   kTeHead = 1u << 26, kTePriv = 1u << 27, kTePad = 0xffffffffu;
+                   kTeHead = 1u << 26, kTePriv = 1u << 27, kTeCont = 1u << 28,
+                   kTePad = 0xffffffffu;
 constexpr uint32_t kStepEntriesMax = kChunkWires;  // padded entries of one step
 constexpr uint32_t kTileWarps = 31;                // consumer warps of a block
 constexpr uint32_t kStepHeaderWords = 16;
