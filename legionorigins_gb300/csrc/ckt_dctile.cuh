@@ -52,6 +52,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0u;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about hint_ns pass, instead of spinning on the barrier.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity,
+                                                    uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0u;
+}
+
 // Orders this thread's earlier shared-memory accesses (generic proxy) before
 // its later bulk copies (async proxy) into the same buffers.
 __device__ __forceinline__ void fence_proxy_async_smem() {
@@ -119,8 +134,7 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar, uint32_t pari
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = dct_now_ns();
   for (;;) {
-    for (int k = 0; k < 16; k++)
-      if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
     if (*abort != 0u || dct_now_ns() - t0 > timeout_ns) return false;
   }
 }
@@ -223,45 +237,68 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     *abort = 0u;
     mbar_init_fence();
   }
-  for (uint32_t i = threadIdx.x; i < nn; i += kTileBlock) {
-    sacc[i] = a.charge[x0 + i];
-    sfold[i] = 0.0f;
+  __syncthreads();
+
+  // Copy warp: the copies of step s into its stage (after the stage's
+  // previous contents have been handed back).
+  uint32_t issued = 0;
+  auto issue = [&](uint32_t s) -> bool {
+    const uint32_t n = s - s0, slot = n % kTileStages;
+    if (n >= kTileStages &&
+        !mbar_wait_abortable(empty + slot, ((n / kTileStages) - 1) & 1u, abort, a.timeout_ns))
+      return false;
+    const uint4 st = a.steps[s];
+    const uint32_t nent = st.y - kStepHeaderWords;
+    uint32_t bytes = st.y * 4, nw = 0;
+    if (st.z != kGatherStep) {
+      nw = (min(kChunkWires, a.W - st.z * kChunkWires) + 3u) & ~3u;
+      bytes += 2 * nw * 4;
+    } else {
+      bytes += nent * 4;
+    }
+    uint64_t *bar = full + slot;
+    fence_proxy_async_smem();
+    mbar_expect_tx(bar, bytes);
+    if (st.z != kGatherStep) {
+      bulk_g2s(vals_of(slot), a.I0 + st.z * kChunkWires, nw * 4, bar);
+      bulk_g2s(vals_of(slot) + kChunkWires, a.I9 + st.z * kChunkWires, nw * 4, bar);
+    } else if (nent > 0) {
+      bulk_g2s(vals_of(slot), a.gw + st.w, nent * 4, bar);
+    }
+    bulk_g2s(block_of(slot), a.ent + st.x, st.y * 4, bar);
+    issued = n + 1;
+    return true;
+  };
+  const bool producer = warp == kTileWarps && lane == 0;
+  uint32_t s_next = s0;
+  if (producer)  // the first stages load while the accumulators fill
+    for (; s_next < min(s1, s0 + kTileStages); s_next++) issue(s_next);
+  {
+    constexpr uint32_t kPer = kTileNodesMax / kTileBlock;
+    float q[kPer];
+#pragma unroll
+    for (uint32_t r = 0; r < kPer; r++) {
+      const uint32_t i = threadIdx.x + r * kTileBlock;
+      q[r] = i < nn ? a.charge[x0 + i] : 0.0f;
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kPer; r++) {
+      const uint32_t i = threadIdx.x + r * kTileBlock;
+      if (i < nn) {
+        sacc[i] = q[r];
+        sfold[i] = 0.0f;
+      }
+    }
   }
   __syncthreads();
 
-  uint32_t issued = 0;  // copy warp: steps issued
   if (warp == kTileWarps) {
-    if (lane == 0) {
-      for (uint32_t s = s0; s < s1; s++) {
-        const uint32_t n = s - s0, slot = n % kTileStages;
-        if (n >= kTileStages &&
-            !mbar_wait_abortable(empty + slot, ((n / kTileStages) - 1) & 1u, abort,
-                                 a.timeout_ns)) {
+    if (producer)
+      for (; s_next < s1; s_next++)
+        if (!issue(s_next)) {
           *abort = 1u;
           break;
         }
-        const uint4 st = a.steps[s];
-        const uint32_t nent = st.y - kStepHeaderWords;
-        uint32_t bytes = st.y * 4, nw = 0;
-        if (st.z != kGatherStep) {
-          nw = (min(kChunkWires, a.W - st.z * kChunkWires) + 3u) & ~3u;
-          bytes += 2 * nw * 4;
-        } else {
-          bytes += nent * 4;
-        }
-        uint64_t *bar = full + slot;
-        fence_proxy_async_smem();
-        mbar_expect_tx(bar, bytes);
-        if (st.z != kGatherStep) {
-          bulk_g2s(vals_of(slot), a.I0 + st.z * kChunkWires, nw * 4, bar);
-          bulk_g2s(vals_of(slot) + kChunkWires, a.I9 + st.z * kChunkWires, nw * 4, bar);
-        } else if (nent > 0) {
-          bulk_g2s(vals_of(slot), a.gw + st.w, nent * 4, bar);
-        }
-        bulk_g2s(block_of(slot), a.ent + st.x, st.y * 4, bar);
-        issued = n + 1;
-      }
-    }
   } else {
     for (uint32_t s = s0; s < s1; s++) {
       const uint32_t n = s - s0, slot = n % kTileStages;
@@ -293,18 +330,41 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     return;
   }
 
-  for (uint32_t i = threadIdx.x; i < nn; i += kTileBlock) {
-    const uint32_t x = x0 + i;
-    const uint32_t o0 = a.off[x], o1 = a.off[x + 1];
+  // The tile's node data in two halves: every load of a half first, then
+  // its stores.
+  constexpr uint32_t kPer = kTileNodesMax / kTileBlock / 2;
+  for (uint32_t h = 0; h < 2; h++) {
+  uint32_t o0[kPer], o1[kPer];
+  float v[kPer], cap[kPer], leak[kPer];
+#pragma unroll
+  for (uint32_t r = 0; r < kPer; r++) {
+    const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
+    o0[r] = o1[r] = 0u;
+    v[r] = 0.0f, cap[r] = 1.0f, leak[r] = 0.0f;
+    if (i < nn) {
+      o0[r] = a.off[x];
+      o1[r] = a.off[x + 1];
+      if (UV) {
+        v[r] = a.voltage[x];
+        cap[r] = a.cap[x];
+        leak[r] = a.leak[x];
+      }
+    }
+  }
+#pragma unroll
+  for (uint32_t r = 0; r < kPer; r++) {
+    const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
+    if (i >= nn) continue;
     float q = sacc[i];
-    if (!(o0 & kPrivateBit) && (o1 & kOffsetMask) > (o0 & kOffsetMask))
+    if (!(o0[r] & kPrivateBit) && (o1[r] & kOffsetMask) > (o0[r] & kOffsetMask))
       q = __fadd_rn(q, sfold[i]);
     if (UV) {
-      a.voltage[x] = uv_one(a.voltage[x], q, a.cap[x], a.leak[x]);
+      a.voltage[x] = uv_one(v[r], q, cap[r], leak[r]);
       a.charge[x] = 0.0f;
     } else {
       a.charge[x] = q;
     }
+  }
   }
 }
 
