@@ -7,13 +7,15 @@
 // consecutive nodes and keeps their running sums in shared memory.  The
 // tile's contributions are grouped by 2048-wire chunk (the plan built with
 // the graph, encoding in ckt_internal.h): for a chunk holding many of them,
-// one thread copies the chunk's I[0] and I[9] slices and the step's entry
-// words into shared memory with cp.async.bulk (completion on an mbarrier),
-// several steps ahead of the threads summing; the few contributions of
-// sparse chunks are gathered directly.  Each node still adds its
-// contributions in CSR order -- private nodes in place, shared and ghost
-// nodes through per-piece folds flushed at group starts -- so the bits
-// equal dc_block's.
+// one lane of a copy warp moves the chunk's I[0] and I[9] slices and the
+// step's entry block into a six-stage shared-memory ring with cp.async.bulk
+// (completion on the stage's mbarrier); the few contributions of sparse
+// chunks are gathered from global memory through staged wire indices.  31
+// consumer warps own disjoint node sets, so they walk the steps without
+// block barriers and hand each stage back through a second mbarrier.  Each
+// node still adds its contributions in CSR order -- private nodes in place,
+// shared and ghost nodes through per-piece folds flushed at group starts --
+// so the bits equal dc_block's.
 #pragma once
 
 #include "ckt_internal.h"
@@ -334,37 +336,37 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   // its stores.
   constexpr uint32_t kPer = kTileNodesMax / kTileBlock / 2;
   for (uint32_t h = 0; h < 2; h++) {
-  uint32_t o0[kPer], o1[kPer];
-  float v[kPer], cap[kPer], leak[kPer];
+    uint32_t o0[kPer], o1[kPer];
+    float v[kPer], cap[kPer], leak[kPer];
 #pragma unroll
-  for (uint32_t r = 0; r < kPer; r++) {
-    const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
-    o0[r] = o1[r] = 0u;
-    v[r] = 0.0f, cap[r] = 1.0f, leak[r] = 0.0f;
-    if (i < nn) {
-      o0[r] = a.off[x];
-      o1[r] = a.off[x + 1];
-      if (UV) {
-        v[r] = a.voltage[x];
-        cap[r] = a.cap[x];
-        leak[r] = a.leak[x];
+    for (uint32_t r = 0; r < kPer; r++) {
+      const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
+      o0[r] = o1[r] = 0u;
+      v[r] = 0.0f, cap[r] = 1.0f, leak[r] = 0.0f;
+      if (i < nn) {
+        o0[r] = a.off[x];
+        o1[r] = a.off[x + 1];
+        if (UV) {
+          v[r] = a.voltage[x];
+          cap[r] = a.cap[x];
+          leak[r] = a.leak[x];
+        }
       }
     }
-  }
 #pragma unroll
-  for (uint32_t r = 0; r < kPer; r++) {
-    const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
-    if (i >= nn) continue;
-    float q = sacc[i];
-    if (!(o0[r] & kPrivateBit) && (o1[r] & kOffsetMask) > (o0[r] & kOffsetMask))
-      q = __fadd_rn(q, sfold[i]);
-    if (UV) {
-      a.voltage[x] = uv_one(v[r], q, cap[r], leak[r]);
-      a.charge[x] = 0.0f;
-    } else {
-      a.charge[x] = q;
+    for (uint32_t r = 0; r < kPer; r++) {
+      const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
+      if (i >= nn) continue;
+      float q = sacc[i];
+      if (!(o0[r] & kPrivateBit) && (o1[r] & kOffsetMask) > (o0[r] & kOffsetMask))
+        q = __fadd_rn(q, sfold[i]);
+      if (UV) {
+        a.voltage[x] = uv_one(v[r], q, cap[r], leak[r]);
+        a.charge[x] = 0.0f;
+      } else {
+        a.charge[x] = q;
+      }
     }
-  }
   }
 }
 
