@@ -8,11 +8,12 @@
 // tile's contributions are grouped by 2048-wire chunk (the plan built with
 // the graph, encoding in ckt_internal.h): for a chunk holding many of them,
 // one lane of a copy warp moves the chunk's I[0] and I[9] slices and the
-// step's entry block into a six-stage shared-memory ring with cp.async.bulk
+// step's entry block into a five-stage shared-memory ring with cp.async.bulk
 // (completion on the stage's mbarrier); the few contributions of sparse
 // chunks are gathered from global memory through staged wire indices.  31
 // consumer warps own disjoint node sets, so they walk the steps without
-// block barriers and hand each stage back through a second mbarrier.  Each
+// block barriers and hand each stage back through a second mbarrier; each
+// lane sums its own list of whole node runs, balanced within the warp.  Each
 // node still adds its contributions in CSR order -- private nodes in place,
 // shared and ghost nodes through per-piece folds flushed at group starts --
 // so the bits equal dc_block's.
@@ -104,7 +105,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 constexpr uint32_t kTileBlock = 32 * (kTileWarps + 1);  // consumer warps + one copy warp
-constexpr uint32_t kTileStages = 6;
+constexpr uint32_t kTileStages = 5;
 // Shared memory of one stage: I[0] and I[9] slices of a chunk (a gather
 // step's wire indices instead), then the step's block (header + entries).
 constexpr uint32_t kStageVals = 2 * kChunkWires;
@@ -145,60 +146,51 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// One warp sums its node runs of a step: entries [b, e) of the step's block,
-// stored 32 runs at a time, round by round (the plan's layout): in a round,
-// lane L takes the next entry of its run at position q + L, and the lanes
-// whose runs continue are a prefix of the warp, counted by a ballot.  Stream
+// One lane sums its list of node runs in a step: entries [b, e) of the
+// step's block, runs back to back, each opened by a head entry.  Stream
 // steps read currents from the staged chunk slices, gather steps from global
-// memory through the staged wire indices.
-__device__ __forceinline__ void dc_tile_warp_walk(const uint32_t *sent, const float *svals,
+// memory through the staged wire indices (loaded ahead of the sums).
+__device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const float *svals,
                                                   uint32_t b, uint32_t e, bool stream,
                                                   const float *__restrict__ I0,
                                                   const float *__restrict__ I9, float *sacc,
-                                                  float *sfold, float dt, uint32_t lane) {
+                                                  float *sfold, float dt) {
   const uint32_t *sgw = reinterpret_cast<const uint32_t *>(svals);
-  uint32_t p = b;
-  while (p < e) {
-    uint32_t u = p + lane < e ? sent[p + lane] : 0u;
-    const bool first = (u & kTeHead) != 0u && u != kTePad;
-    const uint32_t node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
-    float acc = 0.0f, fold = 0.0f;
-    if (first) {
+  uint32_t node = 0xffffffffu;
+  float acc = 0.0f, fold = 0.0f;
+  for (uint32_t p = b; p < e; p++) {
+    const uint32_t u = sent[p];
+    const uint32_t end = (u >> 11) & 1u;
+    float v;
+    if (stream) {
+      v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
+    } else {
+      const uint32_t w = sgw[p];
+      v = end ? I9[w] : I0[w];
+    }
+    if (u & kTeHead) {
+      if (node != 0xffffffffu) {
+        sacc[node] = acc;
+        sfold[node] = fold;
+      }
+      node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
       acc = sacc[node];
       fold = sfold[node];
     }
-    bool mine = first;
-    uint32_t c = __popc(__ballot_sync(0xffffffffu, mine));
-    while (c != 0u) {
-      if (mine) {
-        const uint32_t end = (u >> 11) & 1u;
-        float v;
-        if (stream) {
-          v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
-        } else {
-          const uint32_t w = sgw[p + lane];
-          v = end ? I9[w] : I0[w];
-        }
-        const float cv = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
-        if (u & kTePriv) {
-          acc = __fadd_rn(acc, cv);
-        } else {
-          if (u & kTeFlush) {
-            acc = __fadd_rn(acc, fold);
-            fold = 0.0f;
-          }
-          fold = __fadd_rn(fold, cv);
-        }
+    const float c = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
+    if (u & kTePriv) {
+      acc = __fadd_rn(acc, c);
+    } else {
+      if (u & kTeFlush) {
+        acc = __fadd_rn(acc, fold);
+        fold = 0.0f;
       }
-      p += c;
-      mine = mine && (u & kTeCont) != 0u;
-      c = __popc(__ballot_sync(0xffffffffu, mine));
-      if (mine) u = sent[p + lane];
+      fold = __fadd_rn(fold, c);
     }
-    if (first) {
-      sacc[node] = acc;
-      sfold[node] = fold;
-    }
+  }
+  if (node != 0xffffffffu) {
+    sacc[node] = acc;
+    sfold[node] = fold;
   }
 }
 
@@ -310,11 +302,11 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       }
       const uint32_t *blk = block_of(slot);
       const uint16_t *hdr = reinterpret_cast<const uint16_t *>(blk);
-      const uint32_t last = hdr[2 * kStepHeaderWords - 1];
-      const uint32_t total = last & ~kStepGatherFlag;
-      const uint32_t b = hdr[warp], e = warp + 1 < kTileWarps ? hdr[warp + 1] : total;
-      dc_tile_warp_walk(blk + kStepHeaderWords, vals_of(slot), b, e,
-                        (last & kStepGatherFlag) == 0u, a.I0, a.I9, sacc, sfold, a.dt, lane);
+      const uint32_t last = hdr[kTileLanes];
+      const uint32_t l = threadIdx.x;  // consumer lane list (warp * 32 + lane)
+      const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : last & ~kStepGatherFlag;
+      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e,
+                        (last & kStepGatherFlag) == 0u, a.I0, a.I9, sacc, sfold, a.dt);
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + slot);
     }

@@ -174,27 +174,26 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
   }
   std::sort(keys.begin(), keys.end());
 
-  auto word = [&](uint64_t key, bool head, bool cont) -> uint32_t {
+  auto word = [&](uint64_t key, bool head) -> uint32_t {
     const uint32_t xl = (uint32_t)(key >> 32) & (kTileNodesMax - 1);
     const uint32_t i = lo + (uint32_t)key, x = x0 + xl;
     const uint32_t u = ent[i], w = u >> 2;
     const bool priv = (off[x] & kPrivateBit) != 0;
     const bool flush = !priv && (u & 1u) && i != (off[x] & kOffsetMask);
     return (w % kChunkWires) | ((u & 2u) ? kTeEnd : 0u) | (xl << kTeNodeShift) |
-           (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u) |
-           (cont ? kTeCont : 0u);
+           (flush ? kTeFlush : 0u) | (head ? kTeHead : 0u) | (priv ? kTePriv : 0u);
   };
   // Emits [a, b) of `v` (sorted by node, then CSR position) as one step, or
   // as several when it holds more entries than a step's buffer (a node's
   // entries cut between two steps continue in the later one).  Inside a
   // step, a node's entries form one run, summed by one lane of the warp that
-  // owns the node.  Each warp's runs are taken longest first, 32 at a time
-  // (one per lane), and stored round by round: the first entries of the 32
-  // runs, then the second entries of the runs that have one, and so on, so
-  // that in every round the lanes still busy are a prefix of the warp.
+  // owns the node; each warp deals its runs, longest first, to whichever of
+  // its 32 lanes has the fewest entries so far, so that its lanes finish
+  // together.
   std::vector<std::pair<uint32_t, uint32_t>> runs;  // (length, first index)
   std::vector<uint32_t> order;
   std::vector<std::pair<uint32_t, uint32_t>> wruns[kTileWarps];
+  std::vector<uint32_t> lane_runs[32];
   auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
     const bool gather = chunk == kGatherStep;
     runs.clear();
@@ -224,25 +223,33 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
       }
       const uint32_t b0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
       for (uint32_t h = 0; h < kStepHeaderWords; h++) tp.ent.push_back(0u);
-      uint16_t hdr[2 * kStepHeaderWords] = {};
+      std::vector<uint16_t> hdr(2 * kStepHeaderWords, 0);
       uint32_t n = 0;
       for (uint32_t w = 0; w < kTileWarps; w++) {
-        hdr[w] = (uint16_t)n;
         auto &wr = wruns[w];
         std::stable_sort(wr.begin(), wr.end(),
                          [](const auto &x, const auto &y) { return x.first > y.first; });
-        for (size_t p0 = 0; p0 < wr.size(); p0 += 32) {
-          const size_t p1 = std::min(wr.size(), p0 + 32);
-          for (uint32_t r = 0; r < wr[p0].first; r++)
-            for (size_t k = p0; k < p1 && wr[k].first > r; k++) {
-              const uint32_t j = order[wr[k].second + r];
-              tp.ent.push_back(word(v[j], r == 0, r + 1 < wr[k].first));
+        uint32_t load[32] = {};
+        for (auto &lr : lane_runs) lr.clear();
+        for (uint32_t r = 0; r < (uint32_t)wr.size(); r++) {
+          uint32_t best = 0;
+          for (uint32_t L = 1; L < 32; L++)
+            if (load[L] < load[best]) best = L;
+          load[best] += wr[r].first;
+          lane_runs[best].push_back(r);
+        }
+        for (uint32_t L = 0; L < 32; L++) {
+          hdr[32 * w + L] = (uint16_t)n;
+          for (uint32_t r : lane_runs[L])
+            for (uint32_t k = 0; k < wr[r].first; k++) {
+              const uint32_t j = order[wr[r].second + k];
+              tp.ent.push_back(word(v[j], k == 0));
               if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
               n++;
             }
         }
       }
-      hdr[2 * kStepHeaderWords - 1] = (uint16_t)(n | (gather ? kStepGatherFlag : 0u));
+      hdr[kTileLanes] = (uint16_t)(n | (gather ? kStepGatherFlag : 0u));
       for (uint32_t h = 0; h < kStepHeaderWords; h++)
         tp.ent[b0 + h] = (uint32_t)hdr[2 * h] | ((uint32_t)hdr[2 * h + 1] << 16);
       while ((tp.ent.size() - b0) % 4) {  // 16-byte blocks for the bulk copies

@@ -67,27 +67,27 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 // Steps run in wire order and, inside a step, a node's contributions in
 // wire order, so every node still adds its contributions in the CSR's order.
 // Inside a step, entries are grouped by the consumer warp that owns their
-// node (node within tile mod kTileWarps); a step's block is a header of
-// kStepHeaderWords words -- 32 16-bit offsets: warp w's entries start at
-// header[w] (w < kTileWarps), header[31] = entries | (gather ? 0x8000 : 0)
-// -- followed by the entries, padded to a multiple of 4.
+// node (node within tile mod kTileWarps) and, inside a warp, dealt to its 32
+// lanes as whole runs, longest first to the least-loaded lane.  A step's
+// block is a header of kStepHeaderWords words -- 16-bit offsets: lane list
+// l = 32 w + L starts at header[l] (l < kTileLanes), header[kTileLanes] =
+// entries | (gather ? kStepGatherFlag : 0) -- followed by the entries,
+// padded to a multiple of 4.
 //   step record: {first block word, block words, chunk or kGatherStep,
 //                 first gather-wire slot (parallel to the entries)}
 //   entry word: wire within chunk (11 bits) | end << 11 | node within tile
 //               << 12 (13 bits) | flush << 25 | head << 26 | private << 27
-//               | continues << 28
 // flush: the entry starts a new piece group and is not the node's first;
-// head: first entry of its node within the step; continues: the node has
-// another entry in the step.  Padding words are kTePad.
+// head: first entry of its node within the step.  Padding words are kTePad.
 constexpr uint32_t kTileNodesMax = 8192;
 constexpr uint32_t kChunkWires = 2048;
 constexpr uint32_t kGatherStep = 0xffffffffu;
 constexpr uint32_t kTeEnd = 1u << 11, kTeNodeShift = 12, kTeFlush = 1u << 25,
-                   kTeHead = 1u << 26, kTePriv = 1u << 27, kTeCont = 1u << 28,
-                   kTePad = 0xffffffffu;
+                   kTeHead = 1u << 26, kTePriv = 1u << 27, kTePad = 0xffffffffu;
 constexpr uint32_t kStepEntriesMax = kChunkWires;  // padded entries of one step
 constexpr uint32_t kTileWarps = 31;                // consumer warps of a block
-constexpr uint32_t kStepHeaderWords = 16;
+constexpr uint32_t kTileLanes = 32 * kTileWarps;   // consumer lanes
+constexpr uint32_t kStepHeaderWords = ((kTileLanes + 1 + 1) / 2 + 3) / 4 * 4;
 constexpr uint32_t kStepGatherFlag = 0x8000u;
 
 inline unsigned grid_for(uint64_t n, unsigned block = 256) {
