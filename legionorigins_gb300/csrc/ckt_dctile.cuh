@@ -149,76 +149,49 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // One lane sums its list of node runs in a step: entries [b, e) of the
 // step's block, runs back to back, each opened by a head entry.  Stream
 // steps read currents from the staged chunk slices, gather steps from global
-// memory through the staged wire indices.  Entries go four at a time: their
-// words, their currents and the running sums of the nodes they open are
-// loaded together, then added in order; a run that crosses into the next
-// four carries its sums in registers.
+// memory through the staged wire indices (loaded ahead of the sums).
 __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const float *svals,
                                                   uint32_t b, uint32_t e, bool stream,
                                                   const float *__restrict__ I0,
                                                   const float *__restrict__ I9, float *sacc,
                                                   float *sfold, float dt) {
   const uint32_t *sgw = reinterpret_cast<const uint32_t *>(svals);
-  constexpr uint32_t kU = 4;
   uint32_t node = 0xffffffffu;
   float acc = 0.0f, fold = 0.0f;
-  for (uint32_t p0 = b; p0 < e; p0 += kU) {
-    uint32_t u[kU];
-    float v[kU], ha[kU], hf[kU];
-#pragma unroll
-    for (uint32_t r = 0; r < kU; r++) u[r] = p0 + r < e ? sent[p0 + r] : 0u;
-#pragma unroll
-    for (uint32_t r = 0; r < kU; r++) {
-      const uint32_t end = (u[r] >> 11) & 1u;
-      v[r] = 0.0f;
-      if (p0 + r < e) {
-        if (stream) {
-          v[r] = svals[end * kChunkWires + (u[r] & (kChunkWires - 1))];
-        } else {
-          const uint32_t w = sgw[p0 + r];
-          v[r] = end ? I9[w] : I0[w];
-        }
-      }
-      ha[r] = hf[r] = 0.0f;
-      if (u[r] & kTeHead) {  // a node opened here: no earlier entry of it in this step
-        const uint32_t x = (u[r] >> kTeNodeShift) & (kTileNodesMax - 1);
-        ha[r] = sacc[x];
-        hf[r] = sfold[x];
-      }
+  for (uint32_t p = b; p < e; p++) {
+    const uint32_t u = sent[p];
+    const uint32_t end = (u >> 11) & 1u;
+    float v;
+    if (stream) {
+      v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
+    } else {
+      const uint32_t w = sgw[p];
+      v = end ? I9[w] : I0[w];
     }
-#pragma unroll
-    for (uint32_t r = 0; r < kU; r++) {
-      if (p0 + r >= e) break;
-      if (u[r] & kTeHead) {
-        if (node != 0xffffffffu) {
-          sacc[node] = acc;
-          sfold[node] = fold;
-        }
-        node = (u[r] >> kTeNodeShift) & (kTileNodesMax - 1);
-        acc = ha[r];
-        fold = hf[r];
+    if (u & kTeHead) {
+      if (node != 0xffffffffu) {
+        sacc[node] = acc;
+        sfold[node] = fold;
       }
-      const float c = ((u[r] >> 11) & 1u) ? __fmul_rn(dt, v[r]) : __fmul_rn(-dt, v[r]);
-      if (u[r] & kTePriv) {
-        acc = __fadd_rn(acc, c);
-      } else {
-        if (u[r] & kTeFlush) {
-          acc = __fadd_rn(acc, fold);
-          fold = 0.0f;
-        }
-        fold = __fadd_rn(fold, c);
+      node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
+      acc = sacc[node];
+      fold = sfold[node];
+    }
+    const float c = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
+    if (u & kTePriv) {
+      acc = __fadd_rn(acc, c);
+    } else {
+      if (u & kTeFlush) {
+        acc = __fadd_rn(acc, fold);
+        fold = 0.0f;
       }
+      fold = __fadd_rn(fold, c);
     }
   }
   if (node != 0xffffffffu) {
     sacc[node] = acc;
     sfold[node] = fold;
   }
-}
-
-// Bulk prefetch of [p, p + bytes) into L2 (16-byte aligned start and size).
-__device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 // One block per node tile: warp kTileWarps (lane 0) copies the steps' data
@@ -292,18 +265,8 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   };
   const bool producer = warp == kTileWarps && lane == 0;
   uint32_t s_next = s0;
-  if (producer) {  // the first stages load while the accumulators fill
+  if (producer)  // the first stages load while the accumulators fill
     for (; s_next < min(s1, s0 + kTileStages); s_next++) issue(s_next);
-    // The node data the last pass over the tile reads, into L2 meanwhile.
-    const uint32_t nb = (nn + 1) * 4 & ~15u, vb = nn * 4 & ~15u;
-    if (nb) bulk_prefetch_l2(a.off + x0, nb);
-    if (UV && vb && ((reinterpret_cast<uintptr_t>(a.voltage) | reinterpret_cast<uintptr_t>(a.cap) |
-                      reinterpret_cast<uintptr_t>(a.leak)) & 15u) == 0) {
-      bulk_prefetch_l2(a.voltage + x0, vb);
-      bulk_prefetch_l2(a.cap + x0, vb);
-      bulk_prefetch_l2(a.leak + x0, vb);
-    }
-  }
   {
     constexpr uint32_t kPer = kTileNodesMax / kTileBlock;
     float q[kPer];
