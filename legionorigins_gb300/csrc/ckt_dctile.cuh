@@ -5,10 +5,10 @@
 // at a random wire: every read moves a 32-byte L2 sector for 4 useful bytes,
 // and the sector rate, not DRAM, bounds it.  Here a block owns a tile of
 // consecutive nodes and keeps their running sums in shared memory.  The
-// tile's contributions are grouped by 2048-wire chunk (the plan built with
+// tile's contributions are grouped by 4096-wire chunk (the plan built with
 // the graph, encoding in ckt_internal.h): for a chunk holding many of them,
 // one lane of a copy warp moves the chunk's I[0] and I[9] slices and the
-// step's entry block into a five-stage shared-memory ring with cp.async.bulk
+// step's entry block into a three-stage shared-memory ring with cp.async.bulk
 // (completion on the stage's mbarrier); the few contributions of sparse
 // chunks are gathered from global memory through staged wire indices.  31
 // consumer warps own disjoint node sets, so they walk the steps without
@@ -105,7 +105,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 constexpr uint32_t kTileBlock = 32 * (kTileWarps + 1);  // consumer warps + one copy warp
-constexpr uint32_t kTileStages = 5;
+constexpr uint32_t kTileStages = 3;
 // Shared memory of one stage: I[0] and I[9] slices of a chunk (a gather
 // step's wire indices instead), then the step's block (header + entries).
 constexpr uint32_t kStageVals = 2 * kChunkWires;
@@ -160,7 +160,7 @@ __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const fl
   float acc = 0.0f, fold = 0.0f;
   for (uint32_t p = b; p < e; p++) {
     const uint32_t u = sent[p];
-    const uint32_t end = (u >> 11) & 1u;
+    const uint32_t end = (u & kTeEnd) ? 1u : 0u;
     float v;
     if (stream) {
       v = svals[end * kChunkWires + (u & (kChunkWires - 1))];

@@ -1,5 +1,5 @@
 """The tiled node pass (distribute_charge over node tiles, currents copied
-into shared memory in 2048-wire chunks) against the per-node gather form.
+into shared memory chunk by chunk) against the per-node gather form.
 
 The index-space distribute_charge and the fused node pass take the tiled
 form when the current array is 16-byte aligned and its segment stride is a
@@ -115,13 +115,14 @@ def test_tiled_equals_gather_and_oracle(cuda, oracle, shape, fused):
 
 def test_plan_has_stream_and_gather_steps(cuda, oracle):
     """Config-1 pieces (16384 nodes, 65536 wires each): each half-piece tile
-    copies its piece's 32 chunks (a chunk with more of the tile's entries
-    than a step holds takes two steps) and gathers its ghost contributions."""
+    copies every chunk of its own piece (a chunk with more of the tile's
+    entries than a step holds takes two steps) and gathers its ghost
+    contributions."""
     c = oracle.generate(oracle.GenParams(4, 16384, 65536, 95, 12345, L_offset=0.001))
     dc = Strided(cuda, c, 4 * 65536).dc
     tiles, steps, stream, err = tile_info(dc)
     assert tiles == 8
-    assert 8 * 32 <= stream <= 8 * 64
+    assert 8 * 8 <= stream <= 8 * 64  # chunks of 1024 to 8192 wires
     assert steps > stream
     assert err == 0
 
