@@ -202,7 +202,7 @@ __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const fl
 // update_voltages to the tile's nodes (the fused node pass: charge ends at
 // zero).
 template <bool UV>
-__global__ void __launch_bounds__(kTileBlock, kTileBlock <= 512 ? 2 : 1) dc_tile_kernel(DcTileArgs a) {
+__global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   extern __shared__ __align__(128) unsigned char dct_smem[];
   const uint32_t TN = a.tile_nodes;
   float *sacc = reinterpret_cast<float *>(dct_smem);

@@ -79,8 +79,8 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 //               (13 bits) | flush | head | private, from the low bit up
 // flush: the entry starts a new piece group and is not the node's first;
 // head: first entry of its node within the step.  Padding words are kTePad.
-constexpr uint32_t kTileNodesMax = 4096;
-constexpr uint32_t kChunkBits = 11;
+constexpr uint32_t kTileNodesMax = 8192;
+constexpr uint32_t kChunkBits = 12;
 constexpr uint32_t kChunkWires = 1u << kChunkBits;
 constexpr uint32_t kGatherStep = 0xffffffffu;
 constexpr uint32_t kTeEnd = 1u << kChunkBits, kTeNodeShift = kChunkBits + 1,
@@ -88,7 +88,7 @@ constexpr uint32_t kTeEnd = 1u << kChunkBits, kTeNodeShift = kChunkBits + 1,
                    kTePriv = kTeHead << 1, kTePad = 0xffffffffu;
 constexpr uint32_t kStepEntriesMax = kChunkWires;  // padded entries of one step
 static_assert(kTePriv < (1u << 31), "entry word fields overflow");
-constexpr uint32_t kTileWarps = 15;                // consumer warps of a block
+constexpr uint32_t kTileWarps = 31;                // consumer warps of a block
 constexpr uint32_t kTileLanes = 32 * kTileWarps;   // consumer lanes
 constexpr uint32_t kStepHeaderWords = ((kTileLanes + 1 + 1) / 2 + 3) / 4 * 4;
 constexpr uint32_t kStepGatherFlag = 0x8000u;
