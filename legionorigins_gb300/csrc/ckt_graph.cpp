@@ -43,7 +43,6 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->slot_in);
   cudaFree(g->slot_out);
   cudaFree(g->gstart);
-  cudaFree(g->contrib);
   cudaFree(g->tile_step);
   cudaFree(g->tile_steps);
   cudaFree(g->tile_ent);
@@ -400,7 +399,6 @@ int ckt_graph_create(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_n
       (rc = upload(&g->slot_in, slot_in, &g->device_bytes)) ||
       (rc = upload(&g->slot_out, slot_out, &g->device_bytes)) ||
       (rc = upload(&g->gstart, gstart, &g->device_bytes)) ||
-      (rc = upload(&g->contrib, std::vector<float>(2 * W), &g->device_bytes)) ||
       (rc = build_tile_plan(g, off, ent, kTileNodesMax))) {
     free_graph(g);
     return rc;

@@ -132,11 +132,10 @@ struct ckt_graph {
   uint8_t *touch_loc = nullptr;      // [T]
   uint32_t *touch_off = nullptr;     // [T + 1] into piece_ent
   uint32_t *piece_ent = nullptr;     // [2W]
-  // Two-pass distribute_charge: each wire end's CSR position, a bit per CSR
-  // entry marking the start of a piece group, and the contribution buffer.
+  // Each wire end's CSR position and a bit per CSR entry marking the start
+  // of a piece group (the graph's exported form, ckt_graph_export).
   uint32_t *slot_in = nullptr, *slot_out = nullptr;  // [W]
   uint32_t *gstart = nullptr;                        // [ceil(2W / 32)]
-  float *contrib = nullptr;                          // [2W] scratch
   // Tiled distribute_charge plan (see kTileNodesMax): tile t runs steps
   // [tile_step[t], tile_step[t + 1]).
   uint32_t tile_nodes = 0, num_tiles = 0;
