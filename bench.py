@@ -510,6 +510,30 @@ def main() -> None:
         "traffic": CNC_TRAFFIC_PER_WIRE * shape.W if mode == G.MODE_FAST else None,
         "traffic_unit": "bytes per launch",
     }
+    # A device-to-device copy that moves the same bytes (half read, half
+    # written), timed where the node pass runs -- right after
+    # calc_new_currents, with its dirty lines in L2: what a memory-bound pass
+    # of that size reaches on this GPU, fixed launch and ramp costs included.
+    def same_bytes_copy(nbytes: int) -> float:
+        src = torch.ones(nbytes // 2, dtype=torch.uint8, device=f"cuda:{local}")
+        dst = torch.empty_like(src)
+        ts = []
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                G.check(L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp))
+                a, b = E(), E()
+                a.record(stream)
+                dst.copy_(src)
+                b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+        reset()
+        torch.cuda.synchronize()
+        return statistics.median(ts)
+
+    copy_s = {k: same_bytes_copy(b) for k, b in
+              (("dcuv", 16 * shape.W + 24 * shape.N), ("dc", 16 * shape.W + 8 * shape.N),
+               ("uv", 24 * shape.N))}
     cnc_task_s = statistics.mean(kt_tasks["cnc"])
     kernels = {
         "calc_new_currents": {"ms": 1e3 * cnc_s, "tflops": cnc_flops / cnc_s / 1e12,
@@ -517,6 +541,8 @@ def main() -> None:
         "distribute_update": {"ms": 1e3 * dcuv_s, "algo_bytes": dcuv_bytes,
                               "gbs": dcuv_bytes / dcuv_s / 1e9,
                               "frac_hbm": dcuv_bytes / dcuv_s / 1e9 / hbm,
+                              "same_bytes_copy_ms": 1e3 * copy_s["dcuv"],
+                              "frac_of_same_bytes_copy": copy_s["dcuv"] / dcuv_s,
                               "note": "distribute_charge + update_voltages in one node pass"},
         "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
     }
@@ -527,9 +553,13 @@ def main() -> None:
         "calc_new_currents": {"ms": 1e3 * cnc_task_s,
                               "frac_fp32_peak": cnc_flops / cnc_task_s / peak32},
         "distribute_charge": {"ms": 1e3 * dc_s, "algo_bytes": dc_bytes,
-                              "gbs": dc_bytes / dc_s / 1e9, "frac_hbm": dc_bytes / dc_s / 1e9 / hbm},
+                              "gbs": dc_bytes / dc_s / 1e9, "frac_hbm": dc_bytes / dc_s / 1e9 / hbm,
+                              "same_bytes_copy_ms": 1e3 * copy_s["dc"],
+                              "frac_of_same_bytes_copy": copy_s["dc"] / dc_s},
         "update_voltages": {"ms": 1e3 * uv_s, "algo_bytes": uv_bytes,
-                            "gbs": uv_bytes / uv_s / 1e9, "frac_hbm": uv_bytes / uv_s / 1e9 / hbm},
+                            "gbs": uv_bytes / uv_s / 1e9, "frac_hbm": uv_bytes / uv_s / 1e9 / hbm,
+                            "same_bytes_copy_ms": 1e3 * copy_s["uv"],
+                            "frac_of_same_bytes_copy": copy_s["uv"] / uv_s},
     }
 
     # End to end through the same C-ABI calls with host buffers.
