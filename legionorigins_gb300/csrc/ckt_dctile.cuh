@@ -116,18 +116,29 @@ struct DcTileArgs {
   const uint32_t *tile_step;
   const uint4 *steps;
   const uint32_t *ent, *gw;
-  const uint32_t *off;
+  const uint32_t *mask;  // per tile: nodes whose folds are added at the end
   const float *I0, *I9;  // 16-byte aligned; slices may be read up to a multiple of 4 wires
   float *charge, *voltage;
   const float *cap, *leak;
   uint32_t *error;
   uint64_t timeout_ns;
   uint32_t N, W, tile_nodes;
+  uint32_t node_copy;  // voltage, cap, leak 16-byte aligned: staged by bulk copies
   float dt;
 };
 
+constexpr uint32_t kMaskWords = kTileNodesMax / 32;
+// The last pass reads the tile's voltage, capacitance and leakage from two
+// stages freed by the last steps: stage A holds voltage, then the first
+// kLeakSplit leakages; stage B holds capacitance, then the rest.
+constexpr uint32_t kLeakSplit = kStageBytes / 4 - kTileNodesMax;
+static_assert(kLeakSplit % 4 == 0 && kLeakSplit <= kTileNodesMax &&
+                  kTileNodesMax + (kTileNodesMax - kLeakSplit) <= kStageBytes / 4,
+              "node data does not fit two stages");
+
 __host__ __device__ constexpr uint32_t dc_tile_smem_bytes(uint32_t tile_nodes) {
-  return 2 * tile_nodes * 4 + kTileStages * kStageBytes + 2 * kTileStages * 8 + 16;
+  return 2 * tile_nodes * 4 + kMaskWords * 4 + kTileStages * kStageBytes +
+         (2 * kTileStages + 2) * 8 + 16;
 }
 
 // Bounded wait that also gives up once another thread has raised `abort`.
@@ -207,10 +218,12 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   const uint32_t TN = a.tile_nodes;
   float *sacc = reinterpret_cast<float *>(dct_smem);
   float *sfold = sacc + TN;
-  unsigned char *stage0 = dct_smem + 2 * TN * 4;
+  uint32_t *smask = reinterpret_cast<uint32_t *>(sfold + TN);
+  unsigned char *stage0 = dct_smem + 2 * TN * 4 + kMaskWords * 4;
   uint64_t *full = reinterpret_cast<uint64_t *>(stage0 + kTileStages * kStageBytes);
   uint64_t *empty = full + kTileStages;
-  volatile uint32_t *abort = reinterpret_cast<volatile uint32_t *>(empty + kTileStages);
+  uint64_t *maskbar = empty + kTileStages, *nodebar = maskbar + 1;
+  volatile uint32_t *abort = reinterpret_cast<volatile uint32_t *>(nodebar + 1);
   auto vals_of = [&](uint32_t slot) {
     return reinterpret_cast<float *>(stage0 + slot * kStageBytes);
   };
@@ -228,6 +241,8 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       mbar_init(full + k, 1);
       mbar_init(empty + k, kTileWarps);
     }
+    mbar_init(maskbar, 1);
+    mbar_init(nodebar, 1);
     *abort = 0u;
     mbar_init_fence();
   }
@@ -265,8 +280,20 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   };
   const bool producer = warp == kTileWarps && lane == 0;
   uint32_t s_next = s0;
-  if (producer)  // the first stages load while the accumulators fill
+  if (producer) {  // the fold mask and the first stages load while the accumulators fill
+    fence_proxy_async_smem();
+    mbar_expect_tx(maskbar, kMaskWords * 4);
+    bulk_g2s(smask, a.mask + (size_t)t * kMaskWords, kMaskWords * 4, maskbar);
     for (; s_next < min(s1, s0 + kTileStages); s_next++) issue(s_next);
+  }
+  // Node data staged for the last pass: elements [0, nn4) of each array.
+  const uint32_t nn4 = nn & ~3u, nsteps = s1 - s0;
+  const bool stage_nodes = UV && a.node_copy && nn4 > 0 && nsteps >= 1;
+  uint32_t slot_a = 0, slot_b = 0;
+  if (stage_nodes) {  // the two stages not holding the last step
+    slot_a = (nsteps - 1 + 1) % kTileStages;
+    slot_b = (nsteps - 1 + 2) % kTileStages;
+  }
   {
     constexpr uint32_t kPer = kTileNodesMax / kTileBlock;
     float q[kPer];
@@ -286,13 +313,39 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   }
   __syncthreads();
 
+  bool node_issued = false;
   if (warp == kTileWarps) {
-    if (producer)
+    if (producer) {
       for (; s_next < s1; s_next++)
         if (!issue(s_next)) {
           *abort = 1u;
           break;
         }
+      if (stage_nodes && *abort == 0u) {
+        // Stages A and B last held steps nsteps - 3 and nsteps - 2 (when the
+        // tile has them): wait until the consumers hand them back.
+        bool ok = true;
+        for (uint32_t back = 3; back >= 2 && ok; back--) {
+          if (nsteps < back) continue;
+          const uint32_t n = nsteps - back;
+          ok = mbar_wait_abortable(empty + n % kTileStages, (n / kTileStages) & 1u, abort,
+                                   a.timeout_ns);
+        }
+        if (!ok) {
+          *abort = 1u;
+        } else {
+          float *sa = vals_of(slot_a), *sb = vals_of(slot_b);
+          const uint32_t la = min(nn4, kLeakSplit), lb = nn4 - la;
+          fence_proxy_async_smem();
+          mbar_expect_tx(nodebar, (3 * nn4) * 4);
+          bulk_g2s(sa, a.voltage + x0, nn4 * 4, nodebar);
+          bulk_g2s(sb, a.cap + x0, nn4 * 4, nodebar);
+          bulk_g2s(sa + kTileNodesMax, a.leak + x0, la * 4, nodebar);
+          if (lb) bulk_g2s(sb + kTileNodesMax, a.leak + x0 + la, lb * 4, nodebar);
+          node_issued = true;
+        }
+      }
+    }
   } else {
     for (uint32_t s = s0; s < s1; s++) {
       const uint32_t n = s - s0, slot = n % kTileStages;
@@ -313,51 +366,43 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   }
   __syncthreads();
 
-  if (*abort != 0u) {
+  const bool mask_ok = mbar_wait_bounded(maskbar, 0u, a.timeout_ns);
+  const bool nodes_ok = !stage_nodes || mbar_wait_bounded(nodebar, 0u, a.timeout_ns);
+  if (__syncthreads_or(*abort != 0u || !mask_ok || !nodes_ok)) {
     // A wait ran out: report it, let the copies still in flight land
-    // (bounded), and leave the tile's charges unwritten.
-    if (warp == kTileWarps && lane == 0) {
+    // (bounded), and leave the tile's results unwritten.
+    if (producer) {
       atomicOr(a.error, 1u);
       for (uint32_t n = issued > kTileStages ? issued - kTileStages : 0; n < issued; n++)
         mbar_wait_bounded(full + n % kTileStages, (n / kTileStages) & 1u, a.timeout_ns);
+      if (node_issued) mbar_wait_bounded(nodebar, 0u, a.timeout_ns);
     }
     return;
   }
 
-  // The tile's node data in two halves: every load of a half first, then
-  // its stores.
-  constexpr uint32_t kPer = kTileNodesMax / kTileBlock / 2;
-  for (uint32_t h = 0; h < 2; h++) {
-    uint32_t o0[kPer], o1[kPer];
-    float v[kPer], cap[kPer], leak[kPer];
-#pragma unroll
-    for (uint32_t r = 0; r < kPer; r++) {
-      const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
-      o0[r] = o1[r] = 0u;
-      v[r] = 0.0f, cap[r] = 1.0f, leak[r] = 0.0f;
-      if (i < nn) {
-        o0[r] = a.off[x];
-        o1[r] = a.off[x + 1];
-        if (UV) {
-          v[r] = a.voltage[x];
-          cap[r] = a.cap[x];
-          leak[r] = a.leak[x];
-        }
-      }
-    }
-#pragma unroll
-    for (uint32_t r = 0; r < kPer; r++) {
-      const uint32_t i = threadIdx.x + (h * kPer + r) * kTileBlock, x = x0 + i;
-      if (i >= nn) continue;
-      float q = sacc[i];
-      if (!(o0[r] & kPrivateBit) && (o1[r] & kOffsetMask) > (o0[r] & kOffsetMask))
-        q = __fadd_rn(q, sfold[i]);
-      if (UV) {
-        a.voltage[x] = uv_one(v[r], q, cap[r], leak[r]);
-        a.charge[x] = 0.0f;
+  const float *sv = vals_of(slot_a), *sc = vals_of(slot_b);
+  constexpr uint32_t kPer = kTileNodesMax / kTileBlock;
+#pragma unroll 4
+  for (uint32_t r = 0; r < kPer; r++) {
+    const uint32_t i = threadIdx.x + r * kTileBlock, x = x0 + i;
+    if (i >= nn) break;
+    float q = sacc[i];
+    if ((smask[i >> 5] >> (i & 31u)) & 1u) q = __fadd_rn(q, sfold[i]);
+    if (UV) {
+      float v, cap, leak;
+      if (stage_nodes && i < nn4) {
+        v = sv[i];
+        cap = sc[i];
+        leak = i < kLeakSplit ? sv[kTileNodesMax + i] : sc[kTileNodesMax + i - kLeakSplit];
       } else {
-        a.charge[x] = q;
+        v = a.voltage[x];
+        cap = a.cap[x];
+        leak = a.leak[x];
       }
+      a.voltage[x] = uv_one(v, q, cap, leak);
+      a.charge[x] = 0.0f;
+    } else {
+      a.charge[x] = q;
     }
   }
 }

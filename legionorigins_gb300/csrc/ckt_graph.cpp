@@ -47,6 +47,7 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->tile_steps);
   cudaFree(g->tile_ent);
   cudaFree(g->tile_gw);
+  cudaFree(g->tile_mask);
   cudaFree(g->tile_error);
   delete g;
 }
@@ -316,11 +317,20 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
     std::vector<uint32_t>().swap(plans[t].gw);
   }
   tile_step[T] = (uint32_t)steps.size();
+  // Per tile, the nodes whose folds are added when the tile finishes: not
+  // private and touched by at least one wire.
+  std::vector<uint32_t> mask((size_t)T * (kTileNodesMax / 32), 0u);
+  for (uint32_t x = 0; x < N; x++)
+    if (!(off[x] & kPrivateBit) && (off[x + 1] & kOffsetMask) > (off[x] & kOffsetMask)) {
+      const uint32_t t = x / tile_nodes, i = x % tile_nodes;
+      mask[(size_t)t * (kTileNodesMax / 32) + i / 32] |= 1u << (i % 32);
+    }
   int rc;
   if ((rc = upload(&g->tile_step, tile_step, &g->device_bytes)) ||
       (rc = upload(&g->tile_steps, steps, &g->device_bytes)) ||
       (rc = upload(&g->tile_ent, all_ent, &g->device_bytes)) ||
       (rc = upload(&g->tile_gw, all_gw, &g->device_bytes)) ||
+      (rc = upload(&g->tile_mask, mask, &g->device_bytes)) ||
       (rc = upload(&g->tile_error, std::vector<uint32_t>(1, 0u), &g->device_bytes)))
     return rc;
   g->tile_nodes = tile_nodes;

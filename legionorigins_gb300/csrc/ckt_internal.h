@@ -144,6 +144,8 @@ struct ckt_graph {
   uint4 *tile_steps = nullptr;     // [steps]
   uint32_t *tile_ent = nullptr;    // entry words, every step's run 16-byte aligned
   uint32_t *tile_gw = nullptr;     // gather steps' wire indices, parallel to their entries
+  uint32_t *tile_mask = nullptr;   // [num_tiles * kTileNodesMax / 32] bit: the node's
+                                   // folds are added at the end (shared/ghost, touched)
   uint32_t *tile_error = nullptr;  // [1] bit 0: a copy wait timed out
   int64_t device_bytes = 0;
 };

@@ -130,7 +130,7 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   a.steps = g->tile_steps;
   a.ent = g->tile_ent;
   a.gw = g->tile_gw;
-  a.off = g->node_off;
+  a.mask = g->tile_mask;
   a.I0 = w.current;
   a.I9 = w.current + 9 * w.seg_stride;
   a.charge = n.charge;
@@ -142,6 +142,8 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   a.N = (uint32_t)g->N;
   a.W = (uint32_t)g->W;
   a.tile_nodes = g->tile_nodes;
+  a.node_copy = ((reinterpret_cast<uintptr_t>(n.voltage) | reinterpret_cast<uintptr_t>(n.capacitance) |
+                  reinterpret_cast<uintptr_t>(n.leakage)) & 15u) == 0;
   a.dt = dt;
   dc_tile_kernel<UV><<<g->num_tiles, kTileBlock, dc_tile_smem_bytes(g->tile_nodes), s>>>(a);
   CKT_CHECK_LAUNCH();
