@@ -276,10 +276,14 @@ int ckt_graph_info(const ckt_graph *graph, int64_t *num_wires, int64_t *num_node
 /* The node-tile plan of the index-space distribute_charge and fused node
  * pass (used when wires.current is 16-byte aligned and seg_stride is a
  * multiple of 4): tiles, steps, steps whose current slices are copied whole,
- * and the device error word (bit 0: a copy wait ran out; reading it waits
- * for the device).  No counterpart in the reference. */
+ * and the device error word (bit 0: a copy wait ran out and a tile's
+ * results were left unwritten; reading it waits for the device and clears
+ * it).  No counterpart in the reference. */
 int ckt_graph_tile_info(const ckt_graph *graph, int32_t *tiles, int64_t *steps,
                         int64_t *stream_steps, uint32_t *error_word);
+/* Bound of the tiled pass's waits on its copies, in ns (0: the default, 2 s).
+ * No counterpart in the reference. */
+int ckt_graph_set_tile_timeout(ckt_graph *graph, uint64_t timeout_ns);
 
 /* ------------------------------------------------------------------------
  * Generator: restatement of load_circuit (apps/circuit/circuit.cc:1071-1288)

@@ -148,6 +148,7 @@ SIGNATURES = {
     "ckt_graph_tile_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32),
                                            ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                            ctypes.POINTER(ctypes.c_uint32)]),
+    "ckt_graph_set_tile_timeout": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
     "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
     "ckt_hist_default_params": (None, [ctypes.POINTER(HistParams)]),

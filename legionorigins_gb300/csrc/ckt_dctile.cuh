@@ -369,13 +369,16 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   const bool mask_ok = mbar_wait_bounded(maskbar, 0u, a.timeout_ns);
   const bool nodes_ok = !stage_nodes || mbar_wait_bounded(nodebar, 0u, a.timeout_ns);
   if (__syncthreads_or(*abort != 0u || !mask_ok || !nodes_ok)) {
-    // A wait ran out: report it, let the copies still in flight land
-    // (bounded), and leave the tile's results unwritten.
+    // A wait ran out: report it, let every copy still in flight land (with
+    // a bound of its own, whatever the waits' limit was), and leave the
+    // tile's results unwritten.
     if (producer) {
+      constexpr uint64_t kDrainNs = 1000000000ull;
       atomicOr(a.error, 1u);
+      mbar_wait_bounded(maskbar, 0u, kDrainNs);
       for (uint32_t n = issued > kTileStages ? issued - kTileStages : 0; n < issued; n++)
-        mbar_wait_bounded(full + n % kTileStages, (n / kTileStages) & 1u, a.timeout_ns);
-      if (node_issued) mbar_wait_bounded(nodebar, 0u, a.timeout_ns);
+        mbar_wait_bounded(full + n % kTileStages, (n / kTileStages) & 1u, kDrainNs);
+      if (node_issued) mbar_wait_bounded(nodebar, 0u, kDrainNs);
     }
     return;
   }

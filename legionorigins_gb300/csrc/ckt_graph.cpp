@@ -455,9 +455,17 @@ int ckt_graph_tile_info(const ckt_graph *g, int32_t *tiles, int64_t *steps,
   if (stream_steps) *stream_steps = g->tile_stream_steps;
   if (error_word) {
     *error_word = 0;
-    if (g->tile_error)
+    if (g->tile_error) {
       CKT_CUDA(cudaMemcpy(error_word, g->tile_error, 4, cudaMemcpyDeviceToHost));
+      if (*error_word) CKT_CUDA(cudaMemset(g->tile_error, 0, 4));
+    }
   }
+  return CKT_OK;
+}
+
+int ckt_graph_set_tile_timeout(ckt_graph *g, uint64_t timeout_ns) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  g->tile_timeout_ns = timeout_ns ? timeout_ns : 2000000000ull;
   return CKT_OK;
 }
 

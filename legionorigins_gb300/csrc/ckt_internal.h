@@ -147,5 +147,8 @@ struct ckt_graph {
   uint32_t *tile_mask = nullptr;   // [num_tiles * kTileNodesMax / 32] bit: the node's
                                    // folds are added at the end (shared/ghost, touched)
   uint32_t *tile_error = nullptr;  // [1] bit 0: a copy wait timed out
+  // Bound of the tiled pass's copy waits; a wait that runs out sets the
+  // error word instead of hanging the block.
+  uint64_t tile_timeout_ns = 2000000000ull;
   int64_t device_bytes = 0;
 };

@@ -107,9 +107,6 @@ static bool tile_plan_usable(const ckt_graph *g, const ckt_wires &w) {
          (w.seg_stride & 3) == 0;
 }
 
-// Bound of the tiled pass's copy waits; a wait that runs out sets the
-// graph's error word instead of hanging the block.
-constexpr uint64_t kTileTimeoutNs = 2000000000ull;
 
 template <bool UV>
 static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_nodes &n, float dt,
@@ -138,7 +135,7 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   a.cap = n.capacitance;
   a.leak = n.leakage;
   a.error = g->tile_error;
-  a.timeout_ns = kTileTimeoutNs;
+  a.timeout_ns = g->tile_timeout_ns;
   a.N = (uint32_t)g->N;
   a.W = (uint32_t)g->W;
   a.tile_nodes = g->tile_nodes;

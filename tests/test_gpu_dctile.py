@@ -142,3 +142,77 @@ def test_nan_currents_propagate_identically(cuda, oracle):
     for k in STATE:
         assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
     assert np.isnan(a["node_voltage"]).any()
+
+
+@pytest.mark.parametrize("shape", ["cfg0", "hub", "tiles_straddle_pieces"])
+def test_unaligned_node_arrays(cuda, oracle, shape):
+    """Node arrays that start 4 bytes past a 16-byte boundary: the fused pass
+    reads voltage, capacitance and leakage from global memory instead of
+    staging them by bulk copies; same bits as the aligned arrays."""
+    from legionorigins_gb300 import Nodes, check, lib
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(*SHAPES[shape], L_offset=0.001))
+    W = c.params.num_pieces * c.params.wires_per_piece
+    stride = W + (-W) % 4 + 4
+    a, b = Strided(cuda, c, stride), Strided(cuda, c, stride)
+    N = c.params.num_pieces * c.params.nodes_per_piece
+    off = {}
+    for k, src in (("charge", "charge"), ("node_voltage", "node_voltage"), ("cap", "cap"),
+                   ("leak", "leak")):
+        buf = cuda.zeros(N + 1, dtype=cuda.float32, device="cuda")
+        buf[1:] = b.dc.t[src]
+        off[k] = buf
+    nodes_b = Nodes(off["charge"].data_ptr() + 4, off["node_voltage"].data_ptr() + 4,
+                    off["cap"].data_ptr() + 4, off["leak"].data_ptr() + 4)
+    prm = C.params(2, 0)
+    L = lib()
+    for _ in range(3):
+        check(L.ckt_calc_new_currents_all(a.dc.graph.handle, a.wires(), a.dc.nodes(),
+                                          ctypes.byref(prm), None))
+        check(L.ckt_distribute_update_all(a.dc.graph.handle, a.wires(), a.dc.nodes(),
+                                          ctypes.byref(prm), None))
+        check(L.ckt_calc_new_currents_all(b.dc.graph.handle, b.wires(), nodes_b,
+                                          ctypes.byref(prm), None))
+        check(L.ckt_distribute_update_all(b.dc.graph.handle, b.wires(), nodes_b,
+                                          ctypes.byref(prm), None))
+    cuda.cuda.synchronize()
+    got_a = a.state(cuda)
+    for k, name in (("charge", "charge"), ("node_voltage", "node_voltage")):
+        got_b = off[k][1:].cpu().numpy()
+        assert np.array_equal(got_a[name].view(np.uint32), got_b.view(np.uint32)), (shape, k)
+    for k in ("current", "voltage"):
+        got_b = b.state(cuda)[k]
+        assert np.array_equal(got_a[k].view(np.uint32), got_b.view(np.uint32)), (shape, k)
+    assert tile_info(b.dc)[3] == 0
+
+
+def test_copy_wait_that_runs_out_reports_and_recovers(cuda, oracle):
+    """Waits bounded at 1 ns run out before the copies land: the pass sets
+    the graph's error word (read and cleared through ckt_graph_tile_info),
+    lets its copies land and returns; with the default bound the next pass
+    over the same circuit gives the gather form's bits."""
+    from legionorigins_gb300 import check, lib
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(*SHAPES["tiles_straddle_pieces"], L_offset=0.001))
+    W = c.params.num_pieces * c.params.wires_per_piece
+    stride = W + (-W) % 4 + 4
+    tiled, gather = Strided(cuda, c, stride), Strided(cuda, c, stride + 2)
+    prm = C.params(2, 0)
+    L, g = lib(), tiled.dc.graph.handle
+    check(L.ckt_graph_set_tile_timeout(g, 1))
+    check(L.ckt_distribute_charge_all(g, tiled.wires(), tiled.dc.nodes(), ctypes.byref(prm), None))
+    cuda.cuda.synchronize()
+    assert tile_info(tiled.dc)[3] == 1
+    assert tile_info(tiled.dc)[3] == 0  # cleared by the read
+    check(L.ckt_graph_set_tile_timeout(g, 0))
+    for d in (tiled, gather):
+        for k in ("charge", "node_voltage"):
+            d.dc.t[k].copy_(cuda.from_numpy(np.ascontiguousarray(getattr(c, k))))
+    tiled.loops(prm, 2, True)
+    gather.loops(prm, 2, True)
+    a, b = tiled.state(cuda), gather.state(cuda)
+    for k in STATE:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    assert tile_info(tiled.dc)[3] == 0
