@@ -400,6 +400,7 @@ def main() -> None:
     prm = C.params(INNER_STEPS, mode)
     pristine = {k: dc.t[k].clone() for k in C.STATE_FIELDS}
     g, w, n = dc.graph.handle, dc.wires(), dc.nodes()
+    graph_bytes = dc.graph.info()["device_bytes"]
     E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
     def reset():
@@ -636,7 +637,9 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (reference generator distributions, seed 12345)",
-            "config": workload_config(args.mode, shape.num_pieces), "roofline": roofline,
+            "config": {**workload_config(args.mode, shape.num_pieces),
+                       "graph_device_bytes": graph_bytes},
+            "roofline": roofline,
             "cpu_baseline": cpu_baseline, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "kernels": kernels, "index_space_tasks": index_space_tasks,
             "accuracy": accuracy,
