@@ -29,6 +29,9 @@ SHAPES = {
     "many_pieces_per_tile": (40, 300, 1200, 95, 3),
     "tile_per_piece": (3, 8192, 2048, 90, 5),
     "tiles_straddle_pieces": (2, 20000, 80000, 97, 9),
+    "last_tile_one_node": (1, 8193, 32772, 100, 13),
+    "one_hub_node": (1, 1, 8192, 100, 3),           # 16384 entries of one node, several steps
+    "ragged_wire_count": (3, 50, 333, 80, 17),      # W = 999: the last chunk copy is rounded up
 }
 
 
