@@ -160,7 +160,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // One lane sums its list of node runs in a step: entries [b, e) of the
 // step's block, runs back to back, each opened by a head entry.  Stream
 // steps read currents from the staged chunk slices, gather steps from global
-// memory through the staged wire indices (loaded ahead of the sums).
+// memory at the staged wire indices.
 __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const float *svals,
                                                   uint32_t b, uint32_t e, bool stream,
                                                   const float *__restrict__ I0,
