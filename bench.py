@@ -727,27 +727,32 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
 
     # End to end: every step copies the batch's state in from pinned host
     # memory, runs, and copies it back (topology and constants stay
-    # resident).  Two instances of the batch let one step's upload and the
-    # previous step's download (separate streams: separate copy engines)
-    # overlap a step's launch.
+    # resident).  Three instances of the batch let a step's upload and the
+    # earlier steps' downloads (separate streams: separate copy engines)
+    # overlap the launches: an instance is refilled only once its download
+    # of three steps before has finished, so a slow host link delays no
+    # launch as long as one upload plus one download fits in two launches.
     W, N = info["wires"], info["nodes"]
     hin = [torch.zeros(n, dtype=torch.float32).pin_memory() for n in (10 * W, 9 * W, N, N)]
     G.check(G.lib().ckt_batch_reset_state(b.handle, sp))
     G.check(G.lib().ckt_batch_download_state(b.handle, *[t.data_ptr() for t in hin], sp))
-    houts = [[torch.empty_like(t).pin_memory() for t in hin] for _ in range(2)]
+    n_inst = 3
+    houts = [[torch.empty_like(t).pin_memory() for t in hin] for _ in range(n_inst)]
     torch.cuda.synchronize()
     h2d = sum(t.numel() * 4 for t in hin)
-    b2 = Batch(specs, threads=cpu_threads())
-    b2.set_config(cfg["block"], cfg["wires_per_thread"], cfg["dc_schedule"])
-    pair = [b, b2]
+    extra = [Batch(specs, threads=cpu_threads()) for _ in range(n_inst - 1)]
+    for bx in extra:
+        bx.set_config(cfg["block"], cfg["wires_per_thread"], cfg["dc_schedule"])
+    pair = [b] + extra
     up, down = torch.cuda.Stream(), torch.cuda.Stream()
-    freed = [None, None]
+    freed = [None] * n_inst
 
     def e2e_step(i):
-        bb = pair[i % 2]
+        k = i % n_inst
+        bb = pair[k]
         with torch.cuda.stream(up):
-            if freed[i % 2] is not None:
-                up.wait_event(freed[i % 2])
+            if freed[k] is not None:
+                up.wait_event(freed[k])
             G.check(G.lib().ckt_batch_upload_state(bb.handle, *[t.data_ptr() for t in hin],
                                                    up.cuda_stream))
             loaded = torch.cuda.Event()
@@ -759,9 +764,9 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
         with torch.cuda.stream(down):
             down.wait_event(done)
             G.check(G.lib().ckt_batch_download_state(
-                bb.handle, *[t.data_ptr() for t in houts[i % 2]], down.cuda_stream))
-            freed[i % 2] = torch.cuda.Event()
-            freed[i % 2].record(down)
+                bb.handle, *[t.data_ptr() for t in houts[k]], down.cuda_stream))
+            freed[k] = torch.cuda.Event()
+            freed[k].record(down)
 
     for i in range(args.warmup):
         e2e_step(i)
@@ -776,7 +781,8 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_s = max(e0.elapsed_time(e1) * 1e-3, time.perf_counter() - w0)
-    b2.close()
+    for bx in extra:
+        bx.close()
 
     probe = fp32_peak(torch, G, stream)
     flops = sum(FLOPS_PER_WIRE_STEP * s.wires * s.steps for s in specs)
@@ -813,7 +819,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
             "cpu_baseline": None,
             "e2e": {"value": ws * updates * args.steps / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                    "note": "circuit state in and out every step (topology resident); two "
+                    "note": "circuit state in and out every step (topology resident); three "
                             "batch instances let a step's copies overlap its neighbours' "
                             "launches"},
             "gpu_launches": args.steps, "clocks": clk.summary(),
