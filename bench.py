@@ -768,7 +768,8 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
             freed[k] = torch.cuda.Event()
             freed[k].record(down)
 
-    for i in range(args.warmup):
+    e2e_warm = max(args.warmup, n_inst)  # every instance runs (and builds its graph) once
+    for i in range(e2e_warm):
         e2e_step(i)
     torch.cuda.synchronize()
     e0, e1 = E(), E()
@@ -776,7 +777,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     e0.record(stream)
     up.wait_event(e0)
     for i in range(args.steps):
-        e2e_step(args.warmup + i)
+        e2e_step(e2e_warm + i)
     stream.wait_stream(down)
     e1.record(stream)
     torch.cuda.synchronize()
