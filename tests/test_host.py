@@ -122,6 +122,9 @@ def test_entry_points_validate_arguments(ckt):
     assert L.ckt_distribute_charge_all(None, w, n, ctypes.byref(prm), None) == 1
     assert L.ckt_update_voltages_all(None, n, None) == 1
     assert L.ckt_apply_fold(None, 0, None, None, None, None) == 1
+    assert L.ckt_graph_tile_info(None, None, None, None, None) == 1
+    assert L.ckt_graph_set_tile_timeout(None, 1) == 1
+    assert b"graph is NULL" in L.ckt_last_error()
 
 
 def test_hist_entry_points_validate_arguments(ckt):
