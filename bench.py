@@ -273,6 +273,63 @@ def accuracy_check(torch, G, C, mode) -> dict:
                                                             for k in state))}}
 
 
+def batch_accuracy_check(torch, mode, specs) -> dict:
+    """The same statement for the batched kernel (which the serving rounds
+    run too): the first 8 circuits of the workload's mix, each with 4 inner
+    steps, 2 loops, against the fp64 oracle; and the first 4 at their own
+    inner-step counts, 1 loop, NaN/+-Inf/finite classes against the fp32
+    oracle."""
+    from dataclasses import replace
+
+    from legionorigins_gb300.batch import Batch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ckt_oracle as O
+
+    O.build()
+    state = ("current", "voltage", "charge", "node_voltage")
+
+    def oracle_circuit(sp):
+        return O.generate(O.GenParams(*sp.gen_args()[:5], L_offset=sp.L_offset,
+                                      L_scale=sp.L_scale))
+
+    def cls(a):
+        return np.where(np.isnan(a), 0, np.where(np.isposinf(a), 1, np.where(np.isneginf(a), 2, 3)))
+
+    finite = [replace(sp, steps=4) for sp in specs[:8]]
+    b = Batch(finite)
+    b.run(mode)
+    b.run(mode)
+    torch.cuda.synchronize()
+    rels = []
+    for i, sp in enumerate(finite):
+        got = b.read(i)
+        ref = oracle_circuit(sp).astype(np.float64)
+        O.simulate(ref, 2, sp.steps)
+        rels += [(np.abs(got[k].astype(np.float64) - getattr(ref, k)) /
+                  np.maximum(np.abs(getattr(ref, k)), 1e-6)).ravel() for k in state]
+    b.close()
+    rel = np.concatenate(rels)
+    configured = list(specs[:4])
+    b = Batch(configured)
+    b.run(mode)
+    torch.cuda.synchronize()
+    same = total = 0
+    for i, sp in enumerate(configured):
+        got = b.read(i)
+        ref = oracle_circuit(sp)
+        O.simulate(ref, 1, sp.steps)
+        same += sum(int((cls(got[k]) == cls(getattr(ref, k))).sum()) for k in state)
+        total += sum(got[k].size for k in state)
+    b.close()
+    return {"finite_regime": {"circuits": "the first 8 of the mix, 4 inner steps", "loops": 2,
+                              "max_rel_err_vs_fp64": float(rel.max()),
+                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2)))},
+            "configured_steps": {"circuits": "the first 4 of the mix at their inner steps",
+                                 "loops": 1, "class_match_vs_fp32_oracle": same / total,
+                                 "elements": total}}
+
+
 def fp32_peak(torch, G, stream) -> dict:
     """Measured FP32 FMA throughput (FLOP/s) of this GPU, best of 5, with
     single and with paired (f32x2) FMAs; the roofline uses the larger."""
@@ -818,6 +875,8 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
                          "peak": probe["peak"] / 1e12, "frac": flops / k_mean / probe["peak"],
                          "traffic": None},
             "cpu_baseline": None,
+            "accuracy": (batch_accuracy_check(torch, mode, specs)
+                         if ws == 1 and not args.no_cpu_baseline else None),
             "e2e": {"value": ws * updates * args.steps / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "note": "circuit state in and out every step (topology resident); three "
@@ -1215,6 +1274,12 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
             },
             "latency_ms": quiet["latency_ms"], "latency_at_offered_rps": quiet["offered_rps"],
             "throughput_at_that_rate": quiet["throughput"],
+            # the rounds run the batched kernel: its accuracy on the stream's
+            # first requests of at most 300,000 wires
+            "accuracy": (batch_accuracy_check(
+                torch, mode, [r for r in (serve_request(i) for i in range(200))
+                              if r.wires <= 300_000][:8])
+                         if ws == 1 and not args.no_cpu_baseline else None),
             "capacity_offered_rps": best["offered_rps"], "sweep": sweep,
             "plain_sequential": {
                 "requests": args.serve_plain_sample,
