@@ -253,11 +253,18 @@ def accuracy_check(torch, G, C, mode) -> dict:
     def cls(a):
         return np.where(np.isnan(a), 0, np.where(np.isposinf(a), 1, np.where(np.isneginf(a), 2, 3)))
 
+    def rel_err(a, b):
+        a, b = a.astype(np.float64), b.astype(np.float64)
+        return (np.abs(a - b) / np.maximum(np.abs(b), 1e-6)).ravel()
+
     got = gpu(4, 2)
     ref64 = base.astype(np.float64)
     O.simulate(ref64, 2, 4)
-    rel = np.concatenate([(np.abs(got[k].astype(np.float64) - getattr(ref64, k)) /
-                           np.maximum(np.abs(getattr(ref64, k)), 1e-6)).ravel() for k in state])
+    ref32f = base.copy()
+    O.simulate(ref32f, 2, 4)
+    rel = np.concatenate([rel_err(got[k], getattr(ref64, k)) for k in state])
+    rel32 = np.concatenate([rel_err(got[k], getattr(ref32f, k)) for k in state])
+    refr = np.concatenate([rel_err(getattr(ref32f, k), getattr(ref64, k)) for k in state])
     got_s = gpu(1000, 5)
     ref32 = base.copy()
     O.simulate(ref32, 5, 1000)
@@ -265,7 +272,11 @@ def accuracy_check(torch, G, C, mode) -> dict:
     total = sum(got_s[k].size for k in state)
     return {"finite_regime": {"circuit": "4 x 256 x 1024 (config 0 shape)", "inner_steps": 4,
                               "loops": 2, "max_rel_err_vs_fp64": float(rel.max()),
-                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2)))},
+                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2))),
+                              "max_rel_err_vs_fp32_reference": float(rel32.max()),
+                              "fp32_reference_vs_fp64": {
+                                  "max_rel_err": float(refr.max()),
+                                  "rms_rel_err": float(np.sqrt(np.mean(refr ** 2)))}},
             "configured_steps": {"inner_steps": 1000, "loops": 5,
                                  "class_match_vs_fp32_oracle": same / total,
                                  "elements": total,
@@ -296,20 +307,28 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
     def cls(a):
         return np.where(np.isnan(a), 0, np.where(np.isposinf(a), 1, np.where(np.isneginf(a), 2, 3)))
 
+    def rel_err(a, b):
+        a, b = a.astype(np.float64), b.astype(np.float64)
+        return (np.abs(a - b) / np.maximum(np.abs(b), 1e-6)).ravel()
+
     finite = [replace(sp, steps=4) for sp in specs[:8]]
     b = Batch(finite)
     b.run(mode)
     b.run(mode)
     torch.cuda.synchronize()
-    rels = []
+    rels, rels32, refs = [], [], []
     for i, sp in enumerate(finite):
         got = b.read(i)
-        ref = oracle_circuit(sp).astype(np.float64)
-        O.simulate(ref, 2, sp.steps)
-        rels += [(np.abs(got[k].astype(np.float64) - getattr(ref, k)) /
-                  np.maximum(np.abs(getattr(ref, k)), 1e-6)).ravel() for k in state]
+        ref64 = oracle_circuit(sp).astype(np.float64)
+        O.simulate(ref64, 2, sp.steps)
+        ref32 = oracle_circuit(sp)
+        O.simulate(ref32, 2, sp.steps)
+        for k in state:
+            rels.append(rel_err(got[k], getattr(ref64, k)))
+            rels32.append(rel_err(got[k], getattr(ref32, k)))
+            refs.append(rel_err(getattr(ref32, k), getattr(ref64, k)))
     b.close()
-    rel = np.concatenate(rels)
+    rel, rel32, ref = np.concatenate(rels), np.concatenate(rels32), np.concatenate(refs)
     configured = list(specs[:4])
     b = Batch(configured)
     b.run(mode)
@@ -324,7 +343,14 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
     b.close()
     return {"finite_regime": {"circuits": "the first 8 of the mix, 4 inner steps", "loops": 2,
                               "max_rel_err_vs_fp64": float(rel.max()),
-                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2)))},
+                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2))),
+                              "max_rel_err_vs_fp32_reference": float(rel32.max()),
+                              "fp32_reference_vs_fp64": {
+                                  "max_rel_err": float(ref.max()),
+                                  "rms_rel_err": float(np.sqrt(np.mean(ref ** 2))),
+                                  "note": "the reference's own fp32 arithmetic (the oracle "
+                                          "restating it bit for bit) against fp64: the stiff "
+                                          "recurrence amplifies fp32 rounding"}},
             "configured_steps": {"circuits": "the first 4 of the mix at their inner steps",
                                  "loops": 1, "class_match_vs_fp32_oracle": same / total,
                                  "elements": total}}
