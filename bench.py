@@ -328,7 +328,7 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
             rels32.append(rel_err(got[k], getattr(ref32, k)))
             refs.append(rel_err(getattr(ref32, k), getattr(ref64, k)))
     b.close()
-    rel, rel32, ref = np.concatenate(rels), np.concatenate(rels32), np.concatenate(refs)
+    rel, rel32, refrel = np.concatenate(rels), np.concatenate(rels32), np.concatenate(refs)
     configured = list(specs[:4])
     b = Batch(configured)
     b.run(mode)
@@ -346,8 +346,8 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
                               "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2))),
                               "max_rel_err_vs_fp32_reference": float(rel32.max()),
                               "fp32_reference_vs_fp64": {
-                                  "max_rel_err": float(ref.max()),
-                                  "rms_rel_err": float(np.sqrt(np.mean(ref ** 2))),
+                                  "max_rel_err": float(refrel.max()),
+                                  "rms_rel_err": float(np.sqrt(np.mean(refrel ** 2))),
                                   "note": "the reference's own fp32 arithmetic (the oracle "
                                           "restating it bit for bit) against fp64: the stiff "
                                           "recurrence amplifies fp32 rounding"}},
