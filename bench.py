@@ -316,7 +316,12 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
     b.run(mode)
     b.run(mode)
     torch.cuda.synchronize()
-    rels, rels32, refs = [], [], []
+    def norm_err(a, b):  # per field: ||a - b|| / ||b|| over the finite elements of b
+        a, b = a.astype(np.float64).ravel(), b.astype(np.float64).ravel()
+        f = np.isfinite(b) & np.isfinite(a)
+        return float(np.linalg.norm(a[f] - b[f]) / max(np.linalg.norm(b[f]), 1e-30))
+
+    rels, rels32, refs, norm32 = [], [], [], 0.0
     for i, sp in enumerate(finite):
         got = b.read(i)
         ref64 = oracle_circuit(sp).astype(np.float64)
@@ -327,6 +332,7 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
             rels.append(rel_err(got[k], getattr(ref64, k)))
             rels32.append(rel_err(got[k], getattr(ref32, k)))
             refs.append(rel_err(getattr(ref32, k), getattr(ref64, k)))
+            norm32 = max(norm32, norm_err(got[k], getattr(ref32, k)))
     b.close()
     rel, rel32, refrel = np.concatenate(rels), np.concatenate(rels32), np.concatenate(refs)
     configured = list(specs[:4])
@@ -345,6 +351,7 @@ def batch_accuracy_check(torch, mode, specs) -> dict:
                               "max_rel_err_vs_fp64": float(rel.max()),
                               "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2))),
                               "max_rel_err_vs_fp32_reference": float(rel32.max()),
+                              "max_normwise_err_vs_fp32_reference": norm32,
                               "fp32_reference_vs_fp64": {
                                   "max_rel_err": float(refrel.max()),
                                   "rms_rel_err": float(np.sqrt(np.mean(refrel ** 2))),
