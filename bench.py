@@ -840,28 +840,33 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     def e2e_step(i):
         k = i % n_inst
         bb = pair[k]
+        ev = [E() for _ in range(6)]  # upload, run, download: start and end
         with torch.cuda.stream(up):
             if freed[k] is not None:
                 up.wait_event(freed[k])
+            ev[0].record(up)
             G.check(G.lib().ckt_batch_upload_state(bb.handle, *[t.data_ptr() for t in hin],
                                                    up.cuda_stream))
-            loaded = torch.cuda.Event()
-            loaded.record(up)
-        stream.wait_event(loaded)
+            ev[1].record(up)
+        stream.wait_event(ev[1])
+        ev[2].record(stream)
         bb.run(mode, sp)
-        done = torch.cuda.Event()
-        done.record(stream)
+        ev[3].record(stream)
         with torch.cuda.stream(down):
-            down.wait_event(done)
+            down.wait_event(ev[3])
+            ev[4].record(down)
             G.check(G.lib().ckt_batch_download_state(
                 bb.handle, *[t.data_ptr() for t in houts[k]], down.cuda_stream))
-            freed[k] = torch.cuda.Event()
-            freed[k].record(down)
+            ev[5].record(down)
+            freed[k] = ev[5]
+        e2e_events.append(ev)
 
+    e2e_events = []
     e2e_warm = max(args.warmup, n_inst)  # every instance runs (and builds its graph) once
     for i in range(e2e_warm):
         e2e_step(i)
     torch.cuda.synchronize()
+    e2e_events.clear()
     e0, e1 = E(), E()
     w0 = time.perf_counter()
     e0.record(stream)
@@ -874,6 +879,11 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     e2e_s = max(e0.elapsed_time(e1) * 1e-3, time.perf_counter() - w0)
     for bx in extra:
         bx.close()
+    e2e_parts = {name: statistics.median(ev[2 * j].elapsed_time(ev[2 * j + 1])
+                                         for ev in e2e_events)
+                 for j, name in enumerate(("upload_ms", "run_ms", "download_ms"))}
+    e2e_parts["step_ms"] = 1e3 * e2e_s / max(1, args.steps)
+    e2e_parts["upload_gbs"] = h2d / e2e_parts["upload_ms"] / 1e6
 
     probe = fp32_peak(torch, G, stream)
     flops = sum(FLOPS_PER_WIRE_STEP * s.wires * s.steps for s in specs)
@@ -912,6 +922,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
                          if ws == 1 and not args.no_cpu_baseline else None),
             "e2e": {"value": ws * updates * args.steps / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "parts_median": e2e_parts,
                     "note": "circuit state in and out every step (topology resident); three "
                             "batch instances let a step's copies overlap its neighbours' "
                             "launches"},
