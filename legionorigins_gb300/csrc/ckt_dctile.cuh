@@ -358,67 +358,10 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       const uint32_t last = hdr[kTileLanes];
       const uint32_t l = threadIdx.x;  // consumer lane list (warp * 32 + lane)
       const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : last & ~kStepGatherFlag;
-      const bool stream = (last & kStepGatherFlag) == 0u;
-      const uint32_t *sent = blk + kStepHeaderWords;
-      const float *svals = vals_of(slot);
-      // A list of at most kRegList entries is read into registers (entry
-      // words and currents, or a gather step's wire indices), the stage is
-      // handed back, and the sums run from registers while the copy warp
-      // refills the stage; a longer list is summed from the stage first.
-      constexpr uint32_t kRegList = 8;
-      const uint32_t len = e - b;
-      const bool fits = len <= kRegList;
-      uint32_t u[kRegList], wv[kRegList];
-#pragma unroll
-      for (uint32_t r = 0; r < kRegList; r++) {
-        u[r] = 0u;
-        wv[r] = 0u;
-        if (fits && r < len) {
-          u[r] = sent[b + r];
-          const uint32_t end = (u[r] & kTeEnd) ? 1u : 0u;
-          wv[r] = stream ? __float_as_uint(
-                               svals[end * kChunkWires + (u[r] & (kChunkWires - 1))])
-                         : reinterpret_cast<const uint32_t *>(svals)[b + r];
-        }
-      }
-      if (!fits)
-        dc_tile_lane_walk(sent, svals, b, e, stream, a.I0, a.I9, sacc, sfold, a.dt);
+      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e,
+                        (last & kStepGatherFlag) == 0u, a.I0, a.I9, sacc, sfold, a.dt);
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + slot);
-      if (fits) {
-        uint32_t node = 0xffffffffu;
-        float acc = 0.0f, fold = 0.0f;
-#pragma unroll
-        for (uint32_t r = 0; r < kRegList; r++) {
-          if (r >= len) break;
-          const uint32_t end = (u[r] & kTeEnd) ? 1u : 0u;
-          const float v = stream ? __uint_as_float(wv[r]) : (end ? a.I9[wv[r]] : a.I0[wv[r]]);
-          if (u[r] & kTeHead) {
-            if (node != 0xffffffffu) {
-              sacc[node] = acc;
-              sfold[node] = fold;
-            }
-            node = (u[r] >> kTeNodeShift) & (kTileNodesMax - 1);
-            acc = sacc[node];
-            fold = sfold[node];
-          }
-          const float c = end ? __fmul_rn(a.dt, v) : __fmul_rn(-a.dt, v);
-          if (u[r] & kTePriv) {
-            acc = __fadd_rn(acc, c);
-          } else {
-            if (u[r] & kTeFlush) {
-              acc = __fadd_rn(acc, fold);
-              fold = 0.0f;
-            }
-            fold = __fadd_rn(fold, c);
-          }
-        }
-        if (node != 0xffffffffu) {
-          sacc[node] = acc;
-          sfold[node] = fold;
-        }
-      }
-      __syncwarp();  // this step's sums land before the warp's next step reads them
     }
   }
   __syncthreads();
