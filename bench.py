@@ -51,6 +51,11 @@ import time
 
 import numpy as np
 
+# More hardware work queues than the default 8, so that the separate copy and
+# compute streams of the end-to-end pipelines do not share one queue and
+# wait on each other's unrelated work (set before the CUDA context exists).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
