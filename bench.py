@@ -889,6 +889,10 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
                  for j, name in enumerate(("upload_ms", "run_ms", "download_ms"))}
     e2e_parts["step_ms"] = 1e3 * e2e_s / max(1, args.steps)
     e2e_parts["upload_gbs"] = h2d / e2e_parts["upload_ms"] / 1e6
+    # when each of the first timed steps' copies and launch ran (ms from the
+    # start of the timed region): shows where the pipeline waits
+    e2e_parts["timeline_ms"] = [[round(e0.elapsed_time(x), 1) for x in ev]
+                                for ev in e2e_events[:4]]
 
     probe = fp32_peak(torch, G, stream)
     flops = sum(FLOPS_PER_WIRE_STEP * s.wires * s.steps for s in specs)
