@@ -496,6 +496,10 @@ def main() -> None:
     pristine = {k: dc.t[k].clone() for k in C.STATE_FIELDS}
     g, w, n = dc.graph.handle, dc.wires(), dc.nodes()
     graph_bytes = dc.graph.info()["device_bytes"]
+    tiles = ctypes.c_int32()
+    G.check(L.ckt_graph_tile_info(g, ctypes.byref(tiles), None, None, None))
+    node_pass = ("tiled (dc_tile_kernel)" if tiles.value > 0 and w.current % 16 == 0
+                 and w.seg_stride % 4 == 0 else "gather (dc_all_kernel / dcuv_kernel)")
     E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
     def reset():
@@ -639,6 +643,7 @@ def main() -> None:
                               "frac_hbm": dcuv_bytes / dcuv_s / 1e9 / hbm,
                               "same_bytes_copy_ms": 1e3 * copy_s["dcuv"],
                               "frac_of_same_bytes_copy": copy_s["dcuv"] / dcuv_s,
+                              "form": node_pass,
                               "note": "distribute_charge + update_voltages in one node pass"},
         "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
     }
