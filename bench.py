@@ -381,7 +381,7 @@ def fp32_peak(torch, G, stream) -> dict:
         best = 0.0
         for i in range(6):
             s0.record(stream)
-            G.check(G.lib().ckt_fp32_fma_probe(blocks, iters, paired, sink.data_ptr(),
+            G.check(G.tools().ckt_fp32_fma_probe(blocks, iters, paired, sink.data_ptr(),
                                                stream.cuda_stream))
             s1.record(stream)
             s1.synchronize()

@@ -51,7 +51,12 @@ typedef enum { CKT_PRIVATE_PTR = 0, CKT_SHARED_PTR = 1, CKT_GHOST_PTR = 2 } ckt_
 /* Arithmetic of calc_new_currents. */
 typedef enum {
   /* IEEE fp32 exactly as the reference writes it (correctly rounded
-   * divides, no contraction): bit-identical to the reference CPU task. */
+   * divides, no contraction): bit-identical to the reference CPU task.  Its
+   * divisors (dt, R, C) are loop-invariant, so each wire carries their
+   * reciprocals and every quotient is formed from them and corrected to the
+   * IEEE quotient (Markstein's theorem); dividends where that construction
+   * is not proven exact, and wires whose divisors lie outside its range, use
+   * the divide routine.  Two wires per thread, paired FP32 instructions. */
   CKT_MODE_EXACT = 0,
   /* Loop-invariant quotients L/dt, 1/R and dt/C hoisted out of the inner
    * loop, each current carried before its 1/R scale, fused multiply-adds:
@@ -62,7 +67,11 @@ typedef enum {
   CKT_MODE_FAST = 1,
   /* FAST arithmetic issued one operation per instruction: bit-identical to
    * CKT_MODE_FAST (kept to check the paired forms and to measure them). */
-  CKT_MODE_FAST_SCALAR = 2
+  CKT_MODE_FAST_SCALAR = 2,
+  /* CKT_MODE_EXACT with every quotient from the divide routine, one wire
+   * per thread: the same bits (kept to check CKT_MODE_EXACT and to measure
+   * it against). */
+  CKT_MODE_EXACT_DIVIDE = 3
 } ckt_mode;
 
 /* Wire initialisation of calc_new_currents. */
@@ -491,16 +500,6 @@ int ckt_server_get_stats(ckt_server *server, ckt_server_stats *out);
 double ckt_server_clock(const ckt_server *server);
 /* Stops the threads, abandons open requests and frees everything. */
 int ckt_server_destroy(ckt_server *server);
-
-/* ------------------------------------------------------------------------
- * Measurement helper (no counterpart in the reference): FP32 FMA throughput
- * probe.  Launches `blocks` x 256 threads, each performing iters*16*8
- * independent fused multiply-adds (2 flops each) -- as single FMAs, or with
- * `paired` != 0 as paired (f32x2) FMAs doing two each; time it on `stream`
- * to get the device's FP32-pipe peak.  `sink` is a device float it may
- * write.
- * ---------------------------------------------------------------------- */
-int ckt_fp32_fma_probe(uint32_t blocks, int32_t iters, int32_t paired, float *sink, void *stream);
 
 /* ------------------------------------------------------------------------
  * Reduction microbenchmark: the GPU form of benchmarks/reductions/

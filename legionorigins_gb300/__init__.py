@@ -18,7 +18,7 @@ __all__ = ["lib", "CktError", "Piece", "Wires", "Nodes", "Params", "GenParams", 
 
 LIB_PATH = _build.LIB
 
-MODE_EXACT, MODE_FAST, MODE_FAST_SCALAR = 0, 1, 2
+MODE_EXACT, MODE_FAST, MODE_FAST_SCALAR, MODE_EXACT_DIVIDE = 0, 1, 2, 3
 INIT_KERNEL, INIT_CPU_TASK = 0, 1
 PRIVATE_PTR, SHARED_PTR, GHOST_PTR = 0, 1, 2
 SEGMENTS = 10
@@ -150,7 +150,6 @@ SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_uint32)]),
     "ckt_graph_set_tile_timeout": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "ckt_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(HostCircuit)]),
-    "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
     "ckt_hist_default_params": (None, [ctypes.POINTER(HistParams)]),
     "ckt_hist_scratch_bytes": (ctypes.c_int, [ctypes.POINTER(HistParams), _I32,
                                               ctypes.POINTER(ctypes.c_uint64),
@@ -202,7 +201,33 @@ SIGNATURES = {
     "ckt_server_destroy": (ctypes.c_int, [_P]),
 }
 
+# ... and of include/ckt_tools.h (libckt_tools.so: measurement and
+# verification helpers, not the product library)
+TOOLS_SIGNATURES = {
+    "ckt_fp32_fma_probe": (ctypes.c_int, [_U32, _I32, _I32, _P, _P]),
+    "ckt_check_dt_quotient": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
+    "ckt_check_recip_quotient": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _I32, _I32, _P,
+                                                _P]),
+}
+
 _lib = None
+_tools = None
+
+
+def tools() -> ctypes.CDLL:
+    """Load libckt_tools.so (the FP32 probe and the quotient checks)."""
+    global _tools
+    if _tools is None:
+        lib()
+        if not os.path.exists(_build.TOOLS_LIB):
+            raise RuntimeError(f"{_build.TOOLS_LIB} is not built; run legionorigins_gb300.build.build()")
+        T = ctypes.CDLL(_build.TOOLS_LIB)
+        for name, (res, args) in TOOLS_SIGNATURES.items():
+            fn = getattr(T, name)
+            fn.restype = res
+            fn.argtypes = args
+        _tools = T
+    return _tools
 
 
 def lib(build_if_missing: bool = False) -> ctypes.CDLL:

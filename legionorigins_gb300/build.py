@@ -1,5 +1,6 @@
 """Compile the circuit library (CUDA for sm_103a + host C++) into
-legionorigins_gb300/_build/libckt.so.
+legionorigins_gb300/_build/libckt.so, and the measurement and verification
+helpers of csrc/tools (include/ckt_tools.h) into _build/libckt_tools.so.
 
 nvcc cross-compiles without a GPU, so this runs anywhere the CUDA toolkit
 is installed.  Translation units compile in parallel; the whole build takes
@@ -19,6 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libckt.so")
+TOOLS = os.path.join(CSRC, "tools")
+TOOLS_LIB = os.path.join(BUILD, "libckt_tools.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
@@ -36,15 +39,15 @@ def _cuda_home() -> str:
     raise RuntimeError("CUDA toolkit (nvcc) not found")
 
 
-def sources() -> list[str]:
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+def sources(where: str = CSRC) -> list[str]:
+    return sorted(os.path.join(where, f) for f in os.listdir(where)
                   if f.endswith((".cu", ".cpp")))
 
 
 def _newest_input() -> float:
-    files = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
-                         if f.endswith((".h", ".cuh"))]
-    files.append(os.path.join(INCLUDE, "ckt.h"))
+    files = sources() + sources(TOOLS) + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                                          if f.endswith((".h", ".cuh"))]
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
 
@@ -64,23 +67,34 @@ def _compile(src: str, cuda: str, log: list[str]) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Build libckt.so if any source is newer than it; return its path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    cuda = _cuda_home()
-    log: list[str] = []
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, cuda, log), sources()))
-    tmp = LIB + ".tmp"
-    cmd = [os.path.join(cuda, "bin", "nvcc"), "-shared", *ARCH, "-o", tmp, *objs,
+def _link(out: str, objs: list[str], cuda: str, log: list[str], extra: list[str]) -> None:
+    tmp = out + ".tmp"
+    cmd = [os.path.join(cuda, "bin", "nvcc"), "-shared", *ARCH, "-o", tmp, *objs, *extra,
            "-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     log.append(f"$ {' '.join(cmd)}\n{r.stdout}{r.stderr}")
     if r.returncode != 0:
         raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, out)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Build libckt.so and libckt_tools.so if any source is newer than them;
+    return libckt.so's path."""
+    newest = _newest_input()
+    if not force and all(os.path.exists(p) and os.path.getmtime(p) >= newest
+                         for p in (LIB, TOOLS_LIB)):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cuda = _cuda_home()
+    log: list[str] = []
+    lib_src, tool_src = sources(), sources(TOOLS)
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, cuda, log), lib_src + tool_src))
+    _link(LIB, objs[:len(lib_src)], cuda, log, [])
+    # the tools report errors through libckt.so's ckt_last_error
+    _link(TOOLS_LIB, objs[len(lib_src):], cuda, log,
+          ["-L", BUILD, "-lckt", "-Xlinker", "-rpath=$ORIGIN"])
     with open(os.path.join(BUILD, "build.log"), "w") as f:
         f.write("\n".join(log))
     if verbose:

@@ -168,10 +168,10 @@ __device__ __forceinline__ void dc_contrib_block(const RoundCircuit &rc, uint32_
 
 // DCS: 0 = staged block gather, 1 = one thread per node, 2 = contributions
 // scattered by the CNC tiles then summed contiguously.
-// FAST tiles of two wires per thread run both wires in one paired stepper
+// Tiles of two wires per thread run both wires in one paired stepper
 // (cnc_wire_pair), which needs more registers: two blocks of 256 per SM.
 template <uint32_t BLOCK, int WPT, int DCS, int MODE>
-__global__ void __launch_bounds__(BLOCK, (MODE == CKT_MODE_FAST && WPT == 2 ? 512 : 768) / BLOCK)
+__global__ void __launch_bounds__(BLOCK, (WPT == 2 ? 512 : 768) / BLOCK)
     round_kernel(const BatchItem *__restrict__ items, uint32_t num_items,
                  const RoundCircuit *__restrict__ circ, BatchSync sync, float dt,
                  uint64_t timeout_ns) {
@@ -205,14 +205,14 @@ __global__ void __launch_bounds__(BLOCK, (MODE == CKT_MODE_FAST && WPT == 2 ? 51
       const WireArrays wa = {rc.in_ptr, rc.out_ptr, rc.in_loc, rc.out_loc, rc.L,
                              rc.R,      rc.C,       rc.cur,    rc.vol,     (int64_t)rc.W};
       const NodeVolts volts = {rc.nvolt, rc.nvolt, rc.nvolt};
-      if constexpr (MODE == CKT_MODE_FAST && WPT == 2) {
+      if constexpr (WPT == 2) {
         const uint32_t ta = threadIdx.x, tb = ta + BLOCK;
         if (ta < item.count) {
           const bool has_b = tb < item.count;
           const uint32_t w = item.begin + ta, wb = item.begin + (has_b ? tb : ta);
           float2 i0, i9;
-          cnc_wire_pair<CKT_INIT_KERNEL>((int64_t)w, (int64_t)wb, has_b, wa, volts, rc.steps, dt,
-                                         &i0, &i9);
+          cnc_wire_pair<MODE, CKT_INIT_KERNEL>((int64_t)w, (int64_t)wb, has_b, wa, volts,
+                                               rc.steps, dt, &i0, &i9);
           if (DCS == 2) {
             rc.contrib[rc.slot_in[w]] = __fmul_rn(-dt, i0.x);
             rc.contrib[rc.slot_out[w]] = __fmul_rn(dt, i9.x);

@@ -13,6 +13,7 @@
 #include <cstdint>
 
 #include "ckt.h"
+#include "ckt_divide.cuh"
 
 namespace ckt {
 
@@ -22,9 +23,6 @@ namespace ckt {
 // time-step loop; wire fields are structure-of-arrays so a warp's loads and
 // stores of any one field are one contiguous 128-byte line.
 // ---------------------------------------------------------------------------
-template <int MODE>
-struct WireStep;
-
 // Correctly rounded a / b.  A NaN dividend gives the quiet NaN every GPU
 // arithmetic instruction returns for NaN operands (0x7fffffff, the same bits
 // __fdiv_rn produces) without entering the divide routine's special-case
@@ -33,12 +31,14 @@ __device__ __forceinline__ float div_rn(float a, float b) {
   return (a != a) ? __int_as_float(0x7fffffff) : __fdiv_rn(a, b);
 }
 
-// EXACT: ((dv) - (L*(i-I0))/dt) / R and V0 + (dt*(i_k - i_k+1))/C, each
-// operation rounded exactly as the reference's fp32 source.
-template <>
-struct WireStep<CKT_MODE_EXACT> {
+// EXACT with the divide routine, one wire per thread:
+// ((dv) - (L*(i-I0))/dt) / R and V0 + (dt*(i_k - i_k+1))/C, each operation
+// rounded exactly as the reference's fp32 source.  CKT_MODE_EXACT_DIVIDE, and
+// the wires of CKT_MODE_EXACT whose divisors lie outside the range of the
+// corrected quotients (DualExact below).
+struct DivideStep {
   float L, R, C, dt;
-  __device__ __forceinline__ WireStep(float l, float r, float c, float d) : L(l), R(r), C(c), dt(d) {}
+  __device__ __forceinline__ DivideStep(float l, float r, float c, float d) : L(l), R(r), C(c), dt(d) {}
   __device__ __forceinline__ void step(float (&ni)[10], float (&nv)[11], const float (&I0)[10],
                                        const float (&V0)[9]) const {
 #pragma unroll
@@ -160,6 +160,107 @@ struct DualFast {
   }
 };
 
+// EXACT, two wires per thread: the reference's operations in the reference's
+// order, each rounded as IEEE fp32 rounds it, with the 29 divisions of a
+// wire-step done as correctly rounded quotients by precomputed reciprocals
+// (ckt_divide.cuh) instead of the divide routine.  Wire a's and wire b's
+// operation k share one paired instruction.  A step runs in two phases:
+//   currents:  a1_k = L (i_k - I0_k),  a2_k = (v_k+1 - v_k) - a1_k / dt,
+//              i_k <- a2_k / R
+//   voltages:  a3_k = dt (i_k - i_k+1), v_k+1 <- V0_k + a3_k / C
+// Each phase first forms all of its dividends, then takes the corrected
+// quotients when every dividend of the thread's two wires lies in the
+// guarded range, and the divide routine otherwise (zero dividends, as in a
+// loop's first step, large ones while the recurrence overflows, tiny ones).
+// Both branches round every quotient to the same float, so the bits never
+// depend on which one ran.  DTF: dt is (float)1e-6 and its quotients use the
+// split reciprocal (2 operations); otherwise they are corrected quotients too.
+template <bool DTF>
+struct DualExact {
+  float2 L, dt2, neg1;
+  Recip2 kR, kC, kdt;
+  float dt;
+  __device__ __forceinline__ DualExact(float2 l, float2 r, float2 c, float d) {
+    L = l;
+    dt = d;
+    dt2 = make_float2(d, d);
+    neg1 = make_float2(-1.0f, -1.0f);
+    kR = make_recip2(r.x, r.y);
+    kC = make_recip2(c.x, c.y);
+    if (!DTF) kdt = make_recip2(d, d);
+  }
+  // Both wires' divisors lie in the range the corrected quotients need.
+  static __device__ __forceinline__ bool eligible(float2 r, float2 c, float d) {
+    return divisor_ok(r.x, kRMin, kRMax) && divisor_ok(r.y, kRMin, kRMax) &&
+           divisor_ok(c.x, kCMin, kCMax) && divisor_ok(c.y, kCMin, kCMax) &&
+           (DTF || divisor_ok(d, kCMin, kCMax));
+  }
+  __device__ __forceinline__ float2 dt_div(float2 a) const {
+    if (DTF) return dt_quot2(a);
+    return recip_quot2(a, kdt);
+  }
+  // With DTF no dividend of dt needs a guard of its own: the split quotient
+  // is exact unless |a1| < 2^-118, and then |a1/dt| < 2^-98, far below half
+  // an ulp of any dv with |dv - a1/dt| >= 2^-50 (the guard on a2), so
+  // a2 = RN(dv - a1/dt) = dv either way; when a2's guard fails, the divide
+  // routine recomputes the quotient from a1.
+  __device__ __forceinline__ bool dt_outside(float a) const {
+    if (DTF) return false;
+    return outside(a, kCLo, kCHi);
+  }
+  // ni: currents i_k; nv: voltages v_0..v_10 (v_0, v_10 the node voltages);
+  // nI0 = -I0; V0 = the wire's voltages at the start of the loop.
+  __device__ __forceinline__ void step(float2 (&ni)[10], float2 (&nv)[11],
+                                       const float2 (&nI0)[10], const float2 (&V0)[9]) const {
+    float2 a1[10], a2[10];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      a1[k] = __fmul2_rn(L, __fadd2_rn(ni[k], nI0[k]));
+      const float2 dv = __ffma2_rn(nv[k], neg1, nv[k + 1]);
+      a2[k] = __ffma2_rn(dt_div(a1[k]), neg1, dv);
+      bad |= dt_outside(a1[k].x) | dt_outside(a1[k].y) | outside(a2[k].x, kRLo, kRHi) |
+             outside(a2[k].y, kRLo, kRHi);
+    }
+    if (!bad) {
+#pragma unroll
+      for (int k = 0; k < 10; k++) ni[k] = recip_quot2(a2[k], kR);
+    } else {
+      const float2 R = make_float2(-kR.nb.x, -kR.nb.y);
+#pragma unroll
+      for (int k = 0; k < 10; k++) {
+        const float dx = __fsub_rn(nv[k + 1].x, nv[k].x), dy = __fsub_rn(nv[k + 1].y, nv[k].y);
+        ni[k] = make_float2(__fdiv_rn(__fsub_rn(dx, __fdiv_rn(a1[k].x, dt)), R.x),
+                            __fdiv_rn(__fsub_rn(dy, __fdiv_rn(a1[k].y, dt)), R.y));
+      }
+    }
+    // With DTF, currents from corrected quotients are at most 2^100 / 2^-8
+    // in magnitude, so |a3| <= dt 2^109 < 2^90: only the lower bound needs a
+    // check.  Currents from the divide routine may be anything, so a phase 1
+    // that took it sends phase 2 there too.
+    float2 a3[9];
+    bad = DTF ? bad : false;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a3[k] = __fmul2_rn(dt2, __ffma2_rn(ni[k + 1], neg1, ni[k]));
+      if (DTF)
+        bad |= (fabsf(a3[k].x) < kCLo) | (fabsf(a3[k].y) < kCLo);
+      else
+        bad |= outside(a3[k].x, kCLo, kCHi) | outside(a3[k].y, kCLo, kCHi);
+    }
+    if (!bad) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) nv[k + 1] = __fadd2_rn(V0[k], recip_quot2(a3[k], kC));
+    } else {
+      const float2 C = make_float2(-kC.nb.x, -kC.nb.y);
+#pragma unroll
+      for (int k = 0; k < 9; k++)
+        nv[k + 1] = make_float2(__fadd_rn(V0[k].x, __fdiv_rn(a3[k].x, C.x)),
+                                __fadd_rn(V0[k].y, __fdiv_rn(a3[k].y, C.y)));
+    }
+  }
+};
+
 __device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *pvt,
                                                       const float *shr, const float *ghost) {
   // get_node (apps/circuit/circuit_gpu.cu:40-59) without its assert: a
@@ -259,7 +360,8 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
       for (int k = 0; k < 10; k++) ni[k] = d[k];
     }
   } else {
-    const WireStep<MODE> ws(a.L[w], a.R[w], a.C[w], dt);
+    static_assert(MODE == CKT_MODE_EXACT || MODE == CKT_MODE_EXACT_DIVIDE, "unknown mode");
+    const DivideStep ws(a.L[w], a.R[w], a.C[w], dt);
     int j = 0;
 #pragma unroll 1
     for (; j + 2 <= steps; j += 2) {
@@ -277,22 +379,40 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
   if (i9_out) *i9_out = ni[9];
 }
 
-// FAST mode, two wires per thread (DualFast): thread t of a block handles
-// wires base + t and base + t + 256, so each field's loads and stores stay
-// one contiguous line per warp.  Without a partner wire the thread runs its
-// wire in both lanes and stores one.
-template <int INIT>
+// Two wires per thread (FAST: DualFast, EXACT: DualExact): thread t of a
+// block handles wires base + t and base + t + 256, so each field's loads and
+// stores stay one contiguous line per warp.  Without a partner wire the
+// thread runs its wire in both lanes and stores one.
+template <int MODE, int INIT>
 __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b,
                                               const WireArrays &a, const NodeVolts &nvin,
                                               int steps, float dt, float2 *i0_out = nullptr,
                                               float2 *i9_out = nullptr) {
+  static_assert(MODE == CKT_MODE_FAST || MODE == CKT_MODE_EXACT, "paired modes: FAST, EXACT");
   const int64_t S = a.S;
-  float2 ni[10], nI0[10], nv[11], V0[9];  // ni: d_k during the loop, then the currents
+  const float2 L2 = make_float2(a.L[wa], a.L[wb]), R2 = make_float2(a.R[wa], a.R[wb]),
+               C2 = make_float2(a.C[wa], a.C[wb]);
+  const bool dt_fixed = __float_as_uint(dt) == kDtBits;
+  if (MODE == CKT_MODE_EXACT &&
+      !(dt_fixed ? DualExact<true>::eligible(R2, C2, dt) : DualExact<false>::eligible(R2, C2, dt))) {
+    // a divisor outside the corrected quotients' range: the divide routine
+    float ia0, ia9, ib0, ib9;
+    cnc_wire<CKT_MODE_EXACT_DIVIDE, INIT>(wa, a, nvin, steps, dt, &ia0, &ia9);
+    ib0 = ia0;
+    ib9 = ia9;
+    if (has_b) cnc_wire<CKT_MODE_EXACT_DIVIDE, INIT>(wb, a, nvin, steps, dt, &ib0, &ib9);
+    if (i0_out) *i0_out = make_float2(ia0, ib0);
+    if (i9_out) *i9_out = make_float2(ia9, ib9);
+    return;
+  }
+  // FAST: ni holds d_k = i_k - I0_k during the loop, then the currents;
+  // EXACT: ni holds the currents throughout.
+  float2 ni[10], nI0[10], nv[11], V0[9];
 #pragma unroll
   for (int k = 0; k < 10; k++) {
     const float x = a.cur[k * S + wa], y = a.cur[k * S + wb];
     nI0[k] = make_float2(-x, -y);
-    ni[k] = __fadd2_rn(make_float2(x, y), nI0[k]);
+    ni[k] = MODE == CKT_MODE_FAST ? __fadd2_rn(make_float2(x, y), nI0[k]) : make_float2(x, y);
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) V0[k] = make_float2(a.vol[k * S + wa], a.vol[k * S + wb]);
@@ -309,20 +429,29 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
     nv[9] = make_float2(0.0f, 0.0f);
   }
   nv[10] = make_float2(out_a, out_b);
-  const DualFast pk(make_float2(a.L[wa], a.L[wb]), make_float2(a.R[wa], a.R[wb]),
-                    make_float2(a.C[wa], a.C[wb]), dt);
-  if (steps > 0) {
-    int j = 1;
+  if constexpr (MODE == CKT_MODE_FAST) {
+    const DualFast pk(L2, R2, C2, dt);
+    if (steps > 0) {
+      int j = 1;
 #pragma unroll 1
-    for (; j + 2 <= steps; j += 2) {
-      pk.step<false>(ni, nv, nI0, V0);
-      pk.step<false>(ni, nv, nI0, V0);
-    }
-    if (j < steps) pk.step<false>(ni, nv, nI0, V0);
-    pk.step<true>(ni, nv, nI0, V0);
-  } else {
+      for (; j + 2 <= steps; j += 2) {
+        pk.step<false>(ni, nv, nI0, V0);
+        pk.step<false>(ni, nv, nI0, V0);
+      }
+      if (j < steps) pk.step<false>(ni, nv, nI0, V0);
+      pk.step<true>(ni, nv, nI0, V0);
+    } else {
 #pragma unroll
-    for (int k = 0; k < 10; k++) ni[k] = make_float2(-nI0[k].x, -nI0[k].y);  // no step: I0
+      for (int k = 0; k < 10; k++) ni[k] = make_float2(-nI0[k].x, -nI0[k].y);  // no step: I0
+    }
+  } else if (dt_fixed) {
+    const DualExact<true> pk(L2, R2, C2, dt);
+#pragma unroll 1
+    for (int j = 0; j < steps; j++) pk.step(ni, nv, nI0, V0);
+  } else {
+    const DualExact<false> pk(L2, R2, C2, dt);
+#pragma unroll 1
+    for (int j = 0; j < steps; j++) pk.step(ni, nv, nI0, V0);
   }
 #pragma unroll
   for (int k = 0; k < 10; k++) a.cur[k * S + wa] = ni[k].x;
@@ -340,15 +469,15 @@ __device__ __forceinline__ void cnc_wire_pair(int64_t wa, int64_t wb, bool has_b
 
 constexpr int kPairBlock = 256;  // threads; a block covers 2 * kPairBlock wires
 
-template <int INIT>
+template <int MODE, int INIT>
 __global__ void __launch_bounds__(kPairBlock, 2)
     cnc_pair_kernel(uint32_t first_wire, uint32_t num_wires, WireArrays a, NodeVolts v, int steps,
                     float dt) {
   const uint32_t ta = blockIdx.x * (2 * kPairBlock) + threadIdx.x, tb = ta + kPairBlock;
   if (ta >= num_wires) return;
   const bool has_b = tb < num_wires;
-  cnc_wire_pair<INIT>((int64_t)first_wire + ta, (int64_t)first_wire + (has_b ? tb : ta), has_b,
-                      a, v, steps, dt);
+  cnc_wire_pair<MODE, INIT>((int64_t)first_wire + ta, (int64_t)first_wire + (has_b ? tb : ta),
+                            has_b, a, v, steps, dt);
 }
 
 template <int MODE, int INIT>

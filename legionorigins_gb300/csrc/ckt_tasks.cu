@@ -39,7 +39,7 @@ int validate_params(const ckt_params *p) {
   CKT_REQUIRE(p != nullptr, "params is NULL");
   CKT_REQUIRE(p->steps >= 0, "steps must be >= 0 (got %d)", p->steps);
   CKT_REQUIRE(p->mode == CKT_MODE_EXACT || p->mode == CKT_MODE_FAST ||
-                  p->mode == CKT_MODE_FAST_SCALAR,
+                  p->mode == CKT_MODE_FAST_SCALAR || p->mode == CKT_MODE_EXACT_DIVIDE,
               "unknown mode %d", p->mode);
   CKT_REQUIRE(p->init == CKT_INIT_KERNEL || p->init == CKT_INIT_CPU_TASK, "unknown init %d", p->init);
   return CKT_OK;
@@ -65,9 +65,9 @@ static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const f
                          const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
   const WireArrays a = wire_arrays(w);
   const NodeVolts v = {vp, vs, vg};
-  if (M == CKT_MODE_FAST)  // two wires per thread, every operation paired
-    cnc_pair_kernel<I><<<grid_for(n, 2 * kPairBlock), kPairBlock, 0, s>>>(first, n, a, v,
-                                                                          p->steps, p->dt);
+  if constexpr (M == CKT_MODE_FAST || M == CKT_MODE_EXACT)  // two wires per thread, paired
+    cnc_pair_kernel<M, I><<<grid_for(n, 2 * kPairBlock), kPairBlock, 0, s>>>(first, n, a, v,
+                                                                             p->steps, p->dt);
   else
     cnc_kernel<M, I><<<grid_for(n), 256, 0, s>>>(first, n, a, v, p->steps, p->dt);
 }
@@ -84,9 +84,12 @@ int launch_cnc(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
   } else if (p->mode == CKT_MODE_FAST) {
     if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_FAST, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
     else launch_cnc_t<CKT_MODE_FAST, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
-  } else {
+  } else if (p->mode == CKT_MODE_FAST_SCALAR) {
     if (p->init == CKT_INIT_KERNEL) launch_cnc_t<kModeFastScalar, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
     else launch_cnc_t<kModeFastScalar, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
+  } else {
+    if (p->init == CKT_INIT_KERNEL) launch_cnc_t<CKT_MODE_EXACT_DIVIDE, CKT_INIT_KERNEL>(first, n, w, vp, vs, vg, p, s);
+    else launch_cnc_t<CKT_MODE_EXACT_DIVIDE, CKT_INIT_CPU_TASK>(first, n, w, vp, vs, vg, p, s);
   }
   CKT_CHECK_LAUNCH();
   return CKT_OK;

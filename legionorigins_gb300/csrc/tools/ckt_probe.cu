@@ -3,6 +3,7 @@
 // Eight independent FMA chains per thread keep all four SM sub-partitions'
 // FP32 pipes issuing every cycle.
 #include "ckt_internal.h"
+#include "ckt_tools.h"
 
 namespace ckt {
 

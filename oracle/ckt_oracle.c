@@ -14,6 +14,7 @@
 #define _XOPEN_SOURCE 700
 #include "ckt_oracle.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -690,4 +691,32 @@ double ocl_histogram_threads(uint32_t buckets, uint32_t batch_size, uint32_t num
   free(tid);
   if (failed) return -1.0;
   return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+/* The division by dt of calc_new_currents, L*(new_i - I0)/dt
+ * (apps/circuit/circuit.cc:391-393, circuit_gpu.cu:119-122), as the GPU's
+ * EXACT mode evaluates it: fmaf(a, zh, a*zl) with zh + zl a split
+ * reciprocal of dt.  Compares it with the IEEE quotient a/dt for every float
+ * dividend whose bit pattern lies in [lo, hi) and counts the mismatches among
+ * dividends of magnitude >= tiny (plus zeros, infinities, NaN: trusted) and
+ * among the others; equal means equal bits, or both NaN. */
+void ocl_split_quotient_check(uint64_t lo, uint64_t hi, float dt, float zh, float zl, float tiny,
+                              uint64_t *bad_trusted, uint64_t *bad_other)
+{
+  uint64_t bt = 0, bo = 0;
+  for (uint64_t i = lo; i < hi; i++) {
+    const uint32_t u = (uint32_t)i;
+    float a;
+    memcpy(&a, &u, sizeof a);
+    const float q = fmaf(a, zh, a * zl);
+    const float r = a / dt;
+    uint32_t uq, ur;
+    memcpy(&uq, &q, sizeof uq);
+    memcpy(&ur, &r, sizeof ur);
+    if ((isnan(q) && isnan(r)) || uq == ur) continue;
+    if (!(fabsf(a) < tiny) || a == 0.0f) bt++;
+    else bo++;
+  }
+  *bad_trusted = bt;
+  *bad_other = bo;
 }

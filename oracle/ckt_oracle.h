@@ -20,6 +20,10 @@
  *                       reduction-instance fold/apply order of
  *                       runtime/lowlevel.h:475-492 (pieces applied ascending)
  *   ocl_uv_f32/_f64     apps/circuit/circuit.cc:445-460, :1290-1307
+ *   ocl_split_quotient_check
+ *                       the division by dt of apps/circuit/circuit.cc:391-393
+ *                       as the GPU's EXACT mode forms it (split reciprocal),
+ *                       against IEEE division, over ranges of dividends
  *   ocl_baseline_run    the shared-low-level CPU execution of the same three
  *                       tasks: one pthread per core, piece p on thread p mod T
  *                       (apps/circuit/circuit.cc:623-635), barriers between
@@ -152,6 +156,9 @@ void ocl_histogram(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
 double ocl_histogram_threads(uint32_t buckets, uint32_t batch_size, uint32_t num_batches,
                              uint32_t first_batch, uint32_t seed1, uint32_t seed2,
                              int32_t threads, uint32_t *hist);
+
+void ocl_split_quotient_check(uint64_t lo, uint64_t hi, float dt, float zh, float zl, float tiny,
+                              uint64_t *bad_trusted, uint64_t *bad_other);
 
 #ifdef __cplusplus
 }

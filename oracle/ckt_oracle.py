@@ -89,6 +89,9 @@ def lib():
         L.ocl_histogram.restype = None
         L.ocl_histogram_threads.argtypes = [u32] * 6 + [i32, P]
         L.ocl_histogram_threads.restype = ctypes.c_double
+        f32 = ctypes.c_float
+        L.ocl_split_quotient_check.argtypes = [u64, u64, f32, f32, f32, f32, P, P]
+        L.ocl_split_quotient_check.restype = None
         _lib = L
     return _lib
 
@@ -341,3 +344,12 @@ def run_reducetest(buckets: int, num_batches: int, batch_size: int, workdir: str
             "-bsize", str(batch_size)]
     subprocess.run(args, check=True, env=env, stdout=subprocess.DEVNULL)
     return np.fromfile(path, "<u4")
+
+
+def split_quotient_check(lo: int, hi: int, dt: float, zh: float, zl: float, tiny: float):
+    """Mismatch counts (trusted, other) of fmaf(a, zh, a*zl) against a/dt over
+    the float dividends with bit patterns in [lo, hi); see
+    ocl_split_quotient_check."""
+    bt, bo = ctypes.c_uint64(), ctypes.c_uint64()
+    lib().ocl_split_quotient_check(lo, hi, dt, zh, zl, tiny, ctypes.byref(bt), ctypes.byref(bo))
+    return bt.value, bo.value

@@ -14,9 +14,9 @@ HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.j
            if f.endswith(".h")]
 
 
-def declared_symbols():
+def declared_symbols(headers=None):
     names = set()
-    for h in HEADERS:
+    for h in headers or HEADERS:
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(ckt_\w+)\s*\(", text, re.M):
@@ -24,14 +24,31 @@ def declared_symbols():
     return sorted(names)
 
 
+def test_every_header_is_checked():
+    assert sorted(os.path.basename(h) for h in HEADERS) == ["ckt.h", "ckt_tools.h"]
+
+
 def test_library_exports_every_declared_symbol(ckt):
-    names = declared_symbols()
+    names = declared_symbols([os.path.join(ROOT, "include", "ckt.h")])
     assert len(names) >= 15
     L = ckt.lib()
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
     # ... and the Python binding types every one of them
     assert set(names) <= set(ckt.SIGNATURES), set(names) - set(ckt.SIGNATURES)
+
+
+def test_tools_library_exports_every_declared_symbol(ckt):
+    """The measurement and verification helpers live in their own library,
+    not in the product's."""
+    names = declared_symbols([os.path.join(ROOT, "include", "ckt_tools.h")])
+    assert "ckt_fp32_fma_probe" in names and "ckt_check_dt_quotient" in names
+    T = ckt.tools()
+    missing = [n for n in names if not hasattr(T, n)]
+    assert not missing, missing
+    assert set(names) == set(ckt.TOOLS_SIGNATURES)
+    product = ckt.lib()
+    assert not any(hasattr(product, n) for n in names)
 
 
 def test_abi_version_and_strings(ckt):
