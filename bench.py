@@ -65,6 +65,10 @@ SHAPE = dict(num_pieces=64, nodes_per_piece=16384, wires_per_piece=65536)
 PCT, SEED, INNER_STEPS, OUTER_LOOPS = 95.0, 12345, 1000, 10
 L_OFFSET, L_SCALE = 0.001, 0.01
 FLOPS_PER_WIRE_STEP = 96  # the reference's own count (apps/circuit/circuit.cc:324)
+# FP32-pipe operations calc_new_currents issues per wire-step in its common
+# path: EXACT 67 plain operations + 10 split-reciprocal quotients by dt (2
+# each) + 19 corrected quotients by R and C (4 each); FAST 48.
+FP32_OPS_PER_WIRE_STEP = {0: 163, 1: 48}
 CNC_TRAFFIC_PER_WIRE = (103.879424e6 + 21.284608e6) / 1048576  # measured DRAM bytes per wire
 
 
@@ -231,62 +235,104 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def accuracy_check(torch, G, C, mode) -> dict:
-    """Max and RMS relative error of the GPU loop against the fp64 oracle on
-    the config-0 circuit in the finite regime (4 inner steps x 2 loops), and
-    NaN/+-Inf/finite class agreement with the fp32 oracle at the configured
-    1000 inner steps x 5 loops (where the reference recurrence overflows)."""
+def same_bits(a, b) -> bool:
+    """Bit equality where every NaN equals every NaN (NaN payloads differ
+    between the host ISA and the GPU)."""
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and
+                np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32)))
+
+
+def accuracy_check(torch, G, C, mode, shape_args, configured_steps) -> dict:
+    """The arithmetic this run times, against the oracle (the checker, on the
+    host) on the timed workload's own circuit.
+      finite regime: the whole circuit, 4 inner steps x 2 loops, every value
+        finite: bit equality with the fp32 oracle (the reference's
+        arithmetic), per-element relative error against it and against the
+        fp64 oracle;
+      configured steps: one loop at the configured inner steps (the
+        recurrence overflows to NaN): calc_new_currents on the first piece's
+        wires (each wire is independent given the node voltages),
+        distribute_charge + update_voltages on the whole circuit from the
+        GPU's currents; bit equality and NaN/+-Inf/finite class agreement."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import ckt_oracle as O
 
     O.build()
-    p = O.GenParams(4, 256, 1024, PCT, SEED, L_offset=L_OFFSET, L_scale=L_SCALE)
-    base = O.generate(p)
+    P, npp, wpp, pct = shape_args
+    gp = O.GenParams(P, npp, wpp, pct, SEED, L_offset=L_OFFSET, L_scale=L_SCALE)
+    base = O.generate(gp)
     fields = ("in_ptr", "out_ptr", "in_loc", "out_loc", "L", "R", "C", "current", "voltage",
               "charge", "node_voltage", "cap", "leak", "locator")
     state = ("current", "voltage", "charge", "node_voltage")
+    shape = C.Shape(P, npp, wpp)
 
-    def gpu(steps, loops):
-        dc = C.DeviceCircuit({k: np.ascontiguousarray(getattr(base, k)) for k in fields},
-                             C.Shape(4, 256, 1024))
-        dc.run_loops(C.params(steps, mode), loops)
-        torch.cuda.synchronize()
-        out = dc.to_host()
-        dc.close()
-        return out
+    def device():
+        return C.DeviceCircuit({k: np.ascontiguousarray(getattr(base, k)) for k in fields}, shape)
+
+    def rel(a, b):
+        a, b = a.astype(np.float64).ravel(), b.astype(np.float64).ravel()
+        f = np.isfinite(a) & np.isfinite(b)
+        return np.abs(a[f] - b[f]) / np.maximum(np.abs(b[f]), 1e-6)
 
     def cls(a):
         return np.where(np.isnan(a), 0, np.where(np.isposinf(a), 1, np.where(np.isneginf(a), 2, 3)))
 
-    def rel_err(a, b):
-        a, b = a.astype(np.float64), b.astype(np.float64)
-        return (np.abs(a - b) / np.maximum(np.abs(b), 1e-6)).ravel()
-
-    got = gpu(4, 2)
+    dc = device()
+    dc.run_loops(C.params(4, mode), 2, blocking=True)
+    got = dc.to_host()
+    dc.close()
+    ref32 = base.copy()
+    O.simulate(ref32, 2, 4)
     ref64 = base.astype(np.float64)
     O.simulate(ref64, 2, 4)
-    ref32f = base.copy()
-    O.simulate(ref32f, 2, 4)
-    rel = np.concatenate([rel_err(got[k], getattr(ref64, k)) for k in state])
-    rel32 = np.concatenate([rel_err(got[k], getattr(ref32f, k)) for k in state])
-    refr = np.concatenate([rel_err(getattr(ref32f, k), getattr(ref64, k)) for k in state])
-    got_s = gpu(1000, 5)
-    ref32 = base.copy()
-    O.simulate(ref32, 5, 1000)
-    same = sum(int((cls(got_s[k]) == cls(getattr(ref32, k))).sum()) for k in state)
-    total = sum(got_s[k].size for k in state)
-    return {"finite_regime": {"circuit": "4 x 256 x 1024 (config 0 shape)", "inner_steps": 4,
-                              "loops": 2, "max_rel_err_vs_fp64": float(rel.max()),
-                              "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(rel ** 2))),
-                              "max_rel_err_vs_fp32_reference": float(rel32.max()),
-                              "fp32_reference_vs_fp64": {
-                                  "max_rel_err": float(refr.max()),
-                                  "rms_rel_err": float(np.sqrt(np.mean(refr ** 2)))}},
-            "configured_steps": {"inner_steps": 1000, "loops": 5,
-                                 "class_match_vs_fp32_oracle": same / total,
-                                 "elements": total,
-                                 "finite_elements": int(sum(np.isfinite(got_s[k]).sum()
-                                                            for k in state))}}
+    r32 = np.concatenate([rel(got[k], getattr(ref32, k)) for k in state])
+    r64 = np.concatenate([rel(got[k], getattr(ref64, k)) for k in state])
+    rr = np.concatenate([rel(getattr(ref32, k), getattr(ref64, k)) for k in state])
+    finite = {
+        "circuit": f"{P} x {npp} x {wpp}, {pct:g}% in-piece (the timed circuit, whole)",
+        "inner_steps": 4, "loops": 2,
+        "all_finite": bool(all(np.isfinite(getattr(ref32, k)).all() for k in state)),
+        "bit_identical_to_fp32_reference": all(same_bits(got[k], getattr(ref32, k))
+                                               for k in state),
+        "max_rel_err_vs_fp32_reference": float(r32.max()),
+        "elements_over_1e-5_vs_fp32_reference": int((r32 > 1e-5).sum()),
+        "elements": int(r32.size),
+        "max_rel_err_vs_fp64": float(r64.max()),
+        "rms_rel_err_vs_fp64": float(np.sqrt(np.mean(r64 ** 2))),
+        "fp32_reference_vs_fp64": {"max_rel_err": float(rr.max()),
+                                   "rms_rel_err": float(np.sqrt(np.mean(rr ** 2)))},
+    }
+    dc = device()
+    L = G.lib()
+    prm = C.params(configured_steps, mode)
+    G.check(L.ckt_calc_new_currents_all(dc.graph.handle, dc.wires(), dc.nodes(),
+                                        ctypes.byref(prm), None))
+    torch.cuda.synchronize()
+    after_cnc = dc.to_host()
+    G.check(L.ckt_distribute_update_all_sync(dc.graph.handle, dc.wires(), dc.nodes(),
+                                             ctypes.byref(prm), None))
+    after = dc.to_host()
+    dc.close()
+    ref = base.copy()
+    O.calc_new_currents(ref, configured_steps, w_begin=0, w_end=wpp)
+    c2 = base.copy()
+    c2.current[:], c2.voltage[:] = after_cnc["current"], after_cnc["voltage"]
+    O.distribute_charge(c2)
+    O.update_voltages(c2)
+    pairs = [(after_cnc[k][:, :wpp], getattr(ref, k)[:, :wpp]) for k in ("current", "voltage")]
+    pairs += [(after[k], getattr(c2, k)) for k in ("charge", "node_voltage")]
+    n_el = sum(a.size for a, _ in pairs)
+    configured = {
+        "inner_steps": configured_steps, "loops": 1,
+        "checked": f"calc_new_currents on wires [0, {wpp}) (piece 0); distribute_charge + "
+                   "update_voltages on every node",
+        "bit_identical_to_fp32_reference": all(same_bits(a, b) for a, b in pairs),
+        "class_match_vs_fp32_reference": sum(int((cls(a) == cls(b)).sum()) for a, b in pairs) / n_el,
+        "elements": n_el,
+        "finite_elements": int(sum(np.isfinite(a).sum() for a, _ in pairs)),
+    }
+    return {"finite_regime": finite, "configured_steps": configured}
 
 
 def batch_accuracy_check(torch, mode, specs) -> dict:
@@ -392,12 +438,94 @@ def fp32_peak(torch, G, stream) -> dict:
     return out
 
 
+def plain_measure(torch, G, C, host, shape, mode, inner, loops, steps, warmup, local,
+                  peak32=None, hbm=None) -> dict:
+    """Device-resident timing of one plain workload: a step resets the state
+    by a device copy and runs `loops` outer loops of the library's loop
+    (calc_new_currents, then the fused node pass); then the three separate
+    task launches per loop, for the node kernels' own times.  CUDA events on
+    the launching stream; the tiled pass's error word is checked after every
+    timed section."""
+    L = G.lib()
+    dc = C.DeviceCircuit(host, shape, device=f"cuda:{local}")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    prm = C.params(inner, mode)
+    pristine = {k: dc.t[k].clone() for k in C.STATE_FIELDS}
+    g, w, n = dc.graph.handle, dc.wires(), dc.nodes()
+    E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    ev = {"cnc": [], "dcuv": [], "dc": [], "uv": []}
+    calls = {"fused": (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
+                       ("dcuv", lambda: L.ckt_distribute_update_all(g, w, n, ctypes.byref(prm),
+                                                                    sp))),
+             "tasks": (("cnc", lambda: L.ckt_calc_new_currents_all(g, w, n, ctypes.byref(prm), sp)),
+                       ("dc", lambda: L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), sp)),
+                       ("uv", lambda: L.ckt_update_voltages_all(g, n, sp)))}
+
+    def step(form, record):
+        with torch.cuda.stream(stream):
+            for k in C.STATE_FIELDS:
+                dc.t[k].copy_(pristine[k], non_blocking=True)
+        for _ in range(loops):
+            for name, fn in calls[form]:
+                if record and not (form == "tasks" and name == "cnc"):
+                    a, b = E(), E()
+                    a.record(stream)
+                    G.check(fn())
+                    b.record(stream)
+                    ev[name].append((a, b))
+                else:
+                    G.check(fn())
+
+    for _ in range(warmup):
+        step("fused", False)
+    torch.cuda.synchronize()
+    t0, t1 = E(), E()
+    t0.record(stream)
+    for _ in range(steps):
+        step("fused", True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    G.check(L.ckt_graph_check(g, sp))
+    elapsed = t0.elapsed_time(t1) * 1e-3
+    step("tasks", False)
+    for _ in range(max(1, min(steps, 2))):
+        step("tasks", True)
+    torch.cuda.synchronize()
+    G.check(L.ckt_graph_check(g, sp))
+    dc.close()
+    ms = {k: 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in v) for k, v in ev.items()}
+    W, N = shape.W, shape.N
+    byts = {"dcuv": 16 * W + 24 * N, "dc": 16 * W + 8 * N, "uv": 24 * N}
+    kern = {"calc_new_currents": {"ms": ms["cnc"]}}
+    if peak32:
+        kern["calc_new_currents"]["frac_fp32_peak"] = (FLOPS_PER_WIRE_STEP * W * inner /
+                                                       (ms["cnc"] * 1e-3) / peak32)
+    for name, key in (("distribute_update", "dcuv"), ("distribute_charge", "dc"),
+                      ("update_voltages", "uv")):
+        kern[name] = {"ms": ms[key], "algo_bytes": byts[key],
+                      "gbs": byts[key] / (ms[key] * 1e-3) / 1e9}
+        if hbm:
+            kern[name]["frac_hbm"] = kern[name]["gbs"] / hbm
+    updates = W * 10 * inner * loops * steps
+    return {"value": updates / elapsed, "unit": UNIT, "ms_per_step": 1e3 * elapsed / steps,
+            "steps": steps, "kernels": kern}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--mode", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--mode", choices=["fast", "exact"], default="exact",
+                    help="exact: the reference's fp32 arithmetic bit for bit (the headline); "
+                         "fast: reassociated FMA arithmetic, reported beside it")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="plain workload: skip the config-0/config-2, finite-regime, FAST, "
+                         "batched and served sub-measurements")
+    ap.add_argument("--extra-serve-rates", default="60,120",
+                    help="plain workload: offered request rates (requests/s) of the served "
+                         "sub-measurement")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample-s", type=float, default=3.0,
                     help="target seconds of CPU work per sampled step of the CPU baseline")
@@ -480,11 +608,12 @@ def main() -> None:
         }
 
     # Accuracy of the arithmetic this run uses, stated with the number (the
-    # oracle as the checker, in the CPU leg): the library's loop on the
-    # config-0 circuit (4 x 256 x 1024) against the fp64 and fp32 oracles.
+    # oracle as the checker, on the host): the library's loop on the timed
+    # circuit itself against the fp32 and fp64 oracles.
     accuracy = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        accuracy = accuracy_check(torch, G, C, mode)
+        accuracy = accuracy_check(torch, G, C, mode, (SHAPE["num_pieces"], SHAPE["nodes_per_piece"],
+                                                      SHAPE["wires_per_piece"], PCT), INNER_STEPS)
 
     shape = C.Shape(args.pieces, SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"])
     host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
@@ -551,6 +680,7 @@ def main() -> None:
             step(True)
         t1.record(stream)
         torch.cuda.synchronize()
+    G.check(L.ckt_graph_check(g, sp))  # no tiled pass left a tile unwritten
     barrier()
     from legionorigins_gb300 import replicas
 
@@ -574,6 +704,7 @@ def main() -> None:
         step(True, tasks)
     u1.record(stream)
     torch.cuda.synchronize()
+    G.check(L.ckt_graph_check(g, sp))
     tasks_value = updates_per_step * task_steps / (u0.elapsed_time(u1) * 1e-3)
     kt_tasks = {k: [a.elapsed_time(b) * 1e-3 for a, b in kernel_events[k]]
                 for k in ("cnc", "dc", "uv")}
@@ -604,11 +735,18 @@ def main() -> None:
                        f"{probe['paired'] / 1e12:.1f} TFLOP/s)",
         "algorithmic": f"{FLOPS_PER_WIRE_STEP} flops per wire-step x {shape.W} wires x "
                        f"{INNER_STEPS} steps per launch",
-        # ncu dram__bytes_read.sum + dram__bytes_write.sum of one FAST launch
-        # over 1,048,576 wires (103.9 + 21.3 MB), scaled by the wires: the
-        # traffic is per wire (96 B read, up to 76 B written)
-        "traffic": CNC_TRAFFIC_PER_WIRE * shape.W if mode == G.MODE_FAST else None,
+        # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch over
+        # 1,048,576 wires (103.9 + 21.3 MB), scaled by the wires: the traffic
+        # is per wire (96 B read, up to 76 B written) and the same in every
+        # mode, which load and store the same fields
+        "traffic": CNC_TRAFFIC_PER_WIRE * shape.W,
         "traffic_unit": "bytes per launch",
+        # The reference counts a division as one flop; a correctly rounded
+        # fp32 quotient costs more than one FP32-pipe operation.  The issued
+        # operations per wire-step give the pipe's own utilisation.
+        "issued_fp32_ops_per_wire_step": FP32_OPS_PER_WIRE_STEP[mode],
+        "pipe_frac": (FP32_OPS_PER_WIRE_STEP[mode] * shape.W * INNER_STEPS / cnc_s) /
+                     (peak32 / 2),
     }
     # A device-to-device copy that moves the same bytes (half read, half
     # written), timed where the node pass runs -- right after
@@ -716,6 +854,8 @@ def main() -> None:
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
+    for b_ in bufs:
+        G.check(L.ckt_graph_check(b_[1], sp))
     barrier()
     e2e_total, e2e_s, _ = replicas.aggregate(updates_per_step * args.steps,
                                              max(e0.elapsed_time(e1) * 1e-3, wall), device="cuda")
@@ -723,7 +863,75 @@ def main() -> None:
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "note": "ckt_run_loops_all on host buffers: every step uploads the whole circuit from "
                    "pinned memory and downloads its state; two device copies let one step's "
-                   "copies overlap the neighbouring step's loops"}
+                   "copies overlap the neighbouring step's loops.  The contribution graph and "
+                   "node-tile plan (graph_device_bytes) are built once and stay resident, as "
+                   "the reference's ELAPSED excludes load_circuit (circuit.cc:164-167)"}
+
+    # The other configurations and forms, one GPU: heavy reduction (config
+    # 2), the CPU-runnable shape (config 0), EXACT on a finite-regime state of
+    # the config-1 circuit, FAST mode on config 1 with its error against the
+    # reference's arithmetic, the batched mix (config 3) and the served
+    # request stream (config 4).
+    extras = {}
+    if ws == 1 and not args.no_extras:
+        peak32 = fp32_peak(torch, G, stream)["peak"]
+        hbm_gbs = measured_peaks().get("hbm_gbs") or 6800.0
+        s2 = C.Shape(128, 8192, 32768)
+        h2 = C.generate(128, 8192, 32768, 50.0, SEED, L_OFFSET, L_SCALE)
+        extras["config2"] = {
+            "workload": "heavy reduction: 128 pieces x 8192 nodes x 32768 wires/piece "
+                        "(4,194,304 wires), 50% in-piece, S=500 x 10 loops per step, seed 12345",
+            **plain_measure(torch, G, C, h2, s2, mode, 500, 10, 3, 3, local, peak32, hbm_gbs),
+            "accuracy": (accuracy_check(torch, G, C, mode, (128, 8192, 32768, 50.0), 500)
+                         if not args.no_cpu_baseline else None)}
+        del h2
+        s0 = C.Shape(4, 256, 1024)
+        h0 = C.generate(4, 256, 1024, PCT, SEED, L_OFFSET, L_SCALE)
+        extras["config0"] = {
+            "workload": "CPU-runnable shape: 4 pieces x 256 nodes x 1024 wires/piece, 95% "
+                        "in-piece, S=1000 x 5 loops per step (4,096 wires: 8 blocks, the GPU "
+                        "mostly idle)",
+            **plain_measure(torch, G, C, h0, s0, mode, 1000, 5, 5, 3, local, peak32, hbm_gbs)}
+        conv = {k: v.copy() for k, v in host.items()}
+        rng = np.random.default_rng(1)
+        conv["L"][:] = rng.uniform(1e-7, 9e-7, conv["L"].shape).astype(np.float32)
+        for k, shp in (("current", conv["current"].shape), ("voltage", conv["voltage"].shape),
+                       ("node_voltage", conv["node_voltage"].shape)):
+            conv[k][:] = rng.uniform(-1, 1, shp).astype(np.float32)
+        extras["finite_regime"] = {
+            "workload": "the config-1 circuit with a convergent state (inductance U[1e-7, 9e-7), "
+                        "currents and voltages U[-1, 1)): every value stays finite over the "
+                        "1000 inner steps x 10 loops, so no NaN operand shortens any "
+                        "operation",
+            **plain_measure(torch, G, C, conv, shape, mode, INNER_STEPS, OUTER_LOOPS, 3, 3, local,
+                            peak32, hbm_gbs)}
+        del conv
+        other = G.MODE_FAST if mode == G.MODE_EXACT else G.MODE_EXACT
+        extras["fast_mode" if other == G.MODE_FAST else "exact_mode"] = {
+            "mode": "fast" if other == G.MODE_FAST else "exact",
+            **plain_measure(torch, G, C, host, shape, other, INNER_STEPS, OUTER_LOOPS, 3, 3, local,
+                            peak32, hbm_gbs),
+            "accuracy": (accuracy_check(torch, G, C, other, (SHAPE["num_pieces"],
+                                                             SHAPE["nodes_per_piece"],
+                                                             SHAPE["wires_per_piece"], PCT),
+                                        INNER_STEPS)
+                         if not args.no_cpu_baseline else None),
+            "note": "FAST hoists L/dt, 1/R and dt/C and uses fused multiply-adds: not the "
+                    "reference's rounding, so the stiff recurrence (gain L/(dt R) >> 1) "
+                    "magnifies its one-ulp differences; see its accuracy block"}
+        bres = batched_result(args, torch, G, ws, local, None, mode, 3, 3, piece_sync=False,
+                              accuracy=not args.no_cpu_baseline)
+        extras["batched"] = {k: bres[k] for k in ("value", "unit", "ms_per_step", "config",
+                                                  "plain_sequential", "roofline", "accuracy",
+                                                  "e2e", "clocks", "index_space_frac_fp32_peak")}
+        sres = serve_result(args, torch, G, ws, local, mode,
+                            [float(x) for x in args.extra_serve_rates.split(",") if x], 3.0, 12, 3,
+                            accuracy=not args.no_cpu_baseline)
+        extras["served"] = {k: sres[k] for k in ("value", "unit", "config", "latency_ms",
+                                                 "latency_at_offered_rps",
+                                                 "throughput_at_that_rate",
+                                                 "capacity_offered_rps", "sweep",
+                                                 "plain_sequential", "accuracy", "clocks")}
 
     if rank == 0:
         # the reference app's own report (apps/circuit/circuit.cc:314-333), per
@@ -744,6 +952,7 @@ def main() -> None:
             "clocks": clk.summary(), "kernels": kernels, "index_space_tasks": index_space_tasks,
             "accuracy": accuracy,
             "replicas": "one independent circuit per GPU" if ws > 1 else None,
+            **extras,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -751,12 +960,23 @@ def main() -> None:
 
 
 def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
+    line = batched_result(args, torch, G, ws, local, dist, mode, args.steps, args.warmup,
+                          piece_sync=True, accuracy=ws == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def batched_result(args, torch, G, ws, local, dist, mode, steps, warmup, piece_sync=True,
+                   accuracy=True) -> dict:
     """Batched mixed sizes: 256 independent circuits (pieces U{1..32}, nodes
     per piece log-uniform [256, 16384], 4 wires per node, in-piece fraction
     U[0.8, 0.98], inner steps U{100..1000}, seeds 0..255, one outer loop).
     One step = reset the batch's state, then one persistent launch (CUDA
     graph replay) that runs every circuit's loop.  The plain path on the same
-    circuits (circuit after circuit, three launches each) is timed beside it."""
+    circuits (circuit after circuit, three launches each) is timed beside it;
+    piece_sync adds the reference-shaped per-piece synchronous calls."""
     from legionorigins_gb300.batch import Batch
     from legionorigins_gb300.workloads import mixed_batch
 
@@ -782,7 +1002,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
             events.append((a, z))
         return events
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.reset_state(sp)
         b.run(mode, sp)
     assert b.check(sp) == 0
@@ -792,7 +1012,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     t0, t1 = E(), E()
     with Clocks(local) as clk:
         t0.record(stream)
-        ev = timed(lambda: b.run(mode, sp), args.steps)
+        ev = timed(lambda: b.run(mode, sp), steps)
         t1.record(stream)
         torch.cuda.synchronize()
     if b.check(sp) != 0:
@@ -801,7 +1021,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
 
     if dist is not None:
         dist.barrier()
-    total, elapsed, _ = replicas.aggregate(updates * args.steps, t0.elapsed_time(t1) * 1e-3,
+    total, elapsed, _ = replicas.aggregate(updates * steps, t0.elapsed_time(t1) * 1e-3,
                                            device="cuda")
     kern = [a.elapsed_time(z) * 1e-3 for a, z in ev]
     value = total / elapsed
@@ -813,7 +1033,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
         b.reset_state(sp)
         b.run_sequential(mode, sp, per_piece)
         torch.cuda.synchronize()
-        steps_ = max(1, min(args.steps, 3))
+        steps_ = max(1, min(steps, 3))
         w0 = time.perf_counter()
         for _ in range(steps_):
             G.check(G.lib().ckt_batch_reset_state(b.handle, sp))
@@ -822,7 +1042,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
         return updates * steps_ / (time.perf_counter() - w0)
 
     seq = plain(False)
-    seq_piece = plain(True)
+    seq_piece = plain(True) if piece_sync else None
     pieces_total = sum(s.num_pieces for s in specs)
 
     # End to end: every step copies the batch's state in from pinned host
@@ -872,7 +1092,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
         e2e_events.append(ev)
 
     e2e_events = []
-    e2e_warm = max(args.warmup, n_inst)  # every instance runs (and builds its graph) once
+    e2e_warm = max(warmup, n_inst)  # every instance runs (and builds its graph) once
     for i in range(e2e_warm):
         e2e_step(i)
     torch.cuda.synchronize()
@@ -881,7 +1101,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     w0 = time.perf_counter()
     e0.record(stream)
     up.wait_event(e0)
-    for i in range(args.steps):
+    for i in range(steps):
         e2e_step(e2e_warm + i)
     stream.wait_stream(down)
     e1.record(stream)
@@ -892,7 +1112,7 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     e2e_parts = {name: statistics.median(ev[2 * j].elapsed_time(ev[2 * j + 1])
                                          for ev in e2e_events)
                  for j, name in enumerate(("upload_ms", "run_ms", "download_ms"))}
-    e2e_parts["step_ms"] = 1e3 * e2e_s / max(1, args.steps)
+    e2e_parts["step_ms"] = 1e3 * e2e_s / max(1, steps)
     e2e_parts["upload_gbs"] = h2d / e2e_parts["upload_ms"] / 1e6
     # when each of the first timed steps' copies and launch ran (ms from the
     # start of the timed region): shows where the pipeline waits
@@ -902,10 +1122,10 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
     probe = fp32_peak(torch, G, stream)
     flops = sum(FLOPS_PER_WIRE_STEP * s.wires * s.steps for s in specs)
     k_mean = statistics.mean(kern)
-    if rank == 0:
+    if True:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+            "warmup": warmup, "ms_per_step": 1e3 * elapsed / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (reference generator distributions, seeds 0..255)",
             "config": {
@@ -924,7 +1144,13 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
                                             "launches_per_step": 4 * len(specs)},
                 "per_piece_synchronous": {"value": seq_piece, "unit": UNIT,
                                           "speedup_batched_over_it": value / seq_piece,
-                                          "launches_per_step": 2 * pieces_total + 2 * len(specs)},
+                                          "launches_per_step": 2 * pieces_total + 2 * len(specs)}
+                if seq_piece else None,
+                "ceiling_note": "the plain kernel already runs near the FP32 pipe's limit, so "
+                                "batching can only remove the plain path's idle time between "
+                                "and within per-circuit launches: its ceiling over the "
+                                "index-space path is (plain kernel's fraction of peak) / "
+                                "(index-space path's fraction of peak)",
             },
             "roofline": {"kernel": "batch_kernel (persistent: calc_new_currents + "
                                    "distribute_charge + update_voltages)",
@@ -932,20 +1158,19 @@ def run_batched(args, torch, G, ws, rank, local, dist, mode) -> None:
                          "peak": probe["peak"] / 1e12, "frac": flops / k_mean / probe["peak"],
                          "traffic": None},
             "cpu_baseline": None,
-            "accuracy": (batch_accuracy_check(torch, mode, specs)
-                         if ws == 1 and not args.no_cpu_baseline else None),
-            "e2e": {"value": ws * updates * args.steps / e2e_s, "unit": UNIT,
+            "accuracy": batch_accuracy_check(torch, mode, specs) if accuracy else None,
+            "e2e": {"value": ws * updates * steps / e2e_s, "unit": UNIT,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "parts_median": e2e_parts,
                     "note": "circuit state in and out every step (topology resident); three "
                             "batch instances let a step's copies overlap its neighbours' "
                             "launches"},
-            "gpu_launches": args.steps, "clocks": clk.summary(),
+            "gpu_launches": steps, "clocks": clk.summary(),
         }
-        print(json.dumps(line), flush=True)
     b.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    line["index_space_frac_fp32_peak"] = (flops / (updates / seq) / probe["peak"]
+                                          if seq else None)
+    return line
 
 
 # Reduction microbenchmark (benchmarks/reductions/reducetest.cc): the
@@ -1219,6 +1444,18 @@ def run_layout(args, torch, G, ws, rank, local, dist) -> None:
 
 
 def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
+    rates = [float(x) for x in args.rates.split(",") if x]
+    line = serve_result(args, torch, G, ws, local, mode, rates, args.serve_seconds,
+                        args.serve_plain_sample, args.warmup,
+                        accuracy=ws == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def serve_result(args, torch, G, ws, local, mode, rates, seconds, plain_sample, warmup,
+                 accuracy=True) -> dict:
     """Serving loop: circuit-solve requests arrive as a Poisson stream at each
     offered rate; per request, total wires log-uniform in [1e3, 4e6], 4 wires
     per node, 8..64 pieces, 95% in-piece, inner steps U{100..1000}, 1..5 outer
@@ -1231,11 +1468,10 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
     from legionorigins_gb300.serve import Server
     from legionorigins_gb300.workloads import serve_request
 
-    rates = [float(x) for x in args.rates.split(",") if x]
     sweep = []
     next_id = 0
     warm = Server(mode=mode, prep_threads=cpu_threads())
-    for i in range(args.warmup):
+    for i in range(warmup):
         warm.submit(i, serve_request(10_000_000 + i))
     warm.wait(120.0)
     warm.close()
@@ -1247,7 +1483,7 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
         rng = random.Random(int(rate * 1000) + 7)
         t = 0.0
         arrivals = []
-        while t < args.serve_seconds:
+        while t < seconds:
             t += rng.expovariate(rate)
             arrivals.append(t)
         with Clocks(local) as clk:
@@ -1288,7 +1524,7 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
     plain = {"index_space": [0, 0.0], "per_piece_blocking": [0, 0.0]}
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    for rid in range(args.serve_plain_sample):
+    for rid in range(plain_sample):
         spec = serve_request(rid)
         host = C.generate(*spec.gen_args())
         shape = C.Shape(spec.num_pieces, spec.nodes_per_piece, spec.wires_per_piece)
@@ -1315,10 +1551,10 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
     # (completes >= 95% of the offered rate); above it queueing dominates
     kept = [r for r in sweep if r["completed_rps"] >= 0.95 * r["offered_rps"]]
     quiet = max(kept, key=lambda r: r["offered_rps"]) if kept else min(sweep, key=lambda r: r["offered_rps"])
-    if rank == 0:
+    if True:
         line = {
             "metric": METRIC, "value": best["throughput"], "unit": UNIT, "n_gpus": ws,
-            "steps": len(rates), "warmup": args.warmup,
+            "steps": len(rates), "warmup": warmup,
             "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic request stream (reference generator, seed = request id)",
@@ -1327,7 +1563,7 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
                             "4 wires/node, 8..64 pieces, 95% in-piece, inner steps U{100..1000}, "
                             "outer loops U{1..5}, 80 GB HBM admission budget, continuous "
                             "batching (one persistent launch per round)",
-                "mode": args.mode, "seconds_of_arrivals_per_rate": args.serve_seconds,
+                "mode": args.mode, "seconds_of_arrivals_per_rate": seconds,
                 "rates_rps": rates, "launch": args.serve_launch or "library default",
             },
             "latency_ms": quiet["latency_ms"], "latency_at_offered_rps": quiet["offered_rps"],
@@ -1336,11 +1572,10 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
             # first requests of at most 300,000 wires
             "accuracy": (batch_accuracy_check(
                 torch, mode, [r for r in (serve_request(i) for i in range(200))
-                              if r.wires <= 300_000][:8])
-                         if ws == 1 and not args.no_cpu_baseline else None),
+                              if r.wires <= 300_000][:8]) if accuracy else None),
             "capacity_offered_rps": best["offered_rps"], "sweep": sweep,
             "plain_sequential": {
-                "requests": args.serve_plain_sample,
+                "requests": plain_sample,
                 **{k: {"value": v, "unit": UNIT,
                        "served_over_it": (best["throughput"] / v) if v else None}
                    for k, v in plain_rates.items()},
@@ -1354,9 +1589,7 @@ def run_serve(args, torch, G, ws, rank, local, dist, mode) -> None:
                             "uploaded), and its final state is read back to host memory"},
             "clocks": clk_all[-1] if clk_all else None,
         }
-        print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    return line
 
 
 if __name__ == "__main__":

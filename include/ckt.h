@@ -216,8 +216,9 @@ int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num
  * CKT_NOALLOC_MAX_PIECES slots (24 bytes each, 96 KB) that every GPU loading
  * the library holds until the process exits.
  *  - num_pieces above CKT_NOALLOC_MAX_PIECES is rejected with CKT_EINVAL.
- *  - The first call on a device looks up the array's device address (with
- *    that device current); make that first call before any stream capture.
+ *  - Every call looks up the array's device address on the calling
+ *    thread's current device; the first call on a device also loads the
+ *    library's module there, so make it before any stream capture.
  *  - Every call uses the same array and leaves its contents behind (each
  *    call re-initialises what it reads).  Calls that overlap on the GPU --
  *    other streams, other host threads -- race on it: serialise them.
@@ -250,6 +251,27 @@ int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
                               const ckt_params *prm, void *stream);
 int ckt_run_loops_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                       const ckt_params *prm, int32_t loops, void *stream);
+
+/* Failure of the tiled node pass.  ckt_distribute_charge_all and
+ * ckt_distribute_update_all (and ckt_run_loops_all through them) use a tiled
+ * pass whose copy waits are bounded (ckt_graph_set_tile_timeout).  A wait
+ * that runs out leaves its tile's charges and voltages unwritten and sets the
+ * graph's error word, which lives in host memory mapped for the device:
+ *  - the asynchronous calls cannot know yet whether the pass they launch will
+ *    fail; every later index-space call on the graph returns CKT_ETIMEOUT
+ *    once a finished pass has set the word;
+ *  - ckt_graph_check synchronises `stream`, then returns CKT_ETIMEOUT and
+ *    clears the word if any pass on the graph set it (CKT_OK otherwise);
+ *  - the _sync forms below run the asynchronous call, then ckt_graph_check.
+ * The reference's tasks never fail silently either: their CUDA errors assert
+ * (apps/circuit/circuit_gpu.cu:7-15). */
+int ckt_graph_check(const ckt_graph *graph, void *stream);
+int ckt_distribute_charge_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                                   const ckt_params *prm, void *stream);
+int ckt_distribute_update_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                                   const ckt_params *prm, void *stream);
+int ckt_run_loops_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                           const ckt_params *prm, int32_t loops, void *stream);
 
 /* ------------------------------------------------------------------------
  * Reference-instance interop: conversion between the reference's
@@ -285,9 +307,9 @@ int ckt_graph_info(const ckt_graph *graph, int64_t *num_wires, int64_t *num_node
 /* The node-tile plan of the index-space distribute_charge and fused node
  * pass (used when wires.current is 16-byte aligned and seg_stride is a
  * multiple of 4): tiles, steps, steps whose current slices are copied whole,
- * and the device error word (bit 0: a copy wait ran out and a tile's
- * results were left unwritten; reading it waits for the device and clears
- * it).  No counterpart in the reference. */
+ * and the error word (bit 0: a copy wait ran out and a tile's results were
+ * left unwritten; reading it waits for the whole device and clears it).  No
+ * counterpart in the reference. */
 int ckt_graph_tile_info(const ckt_graph *graph, int32_t *tiles, int64_t *steps,
                         int64_t *stream_steps, uint32_t *error_word);
 /* Bound of the tiled pass's waits on its copies, in ns (0: the default, 2 s).

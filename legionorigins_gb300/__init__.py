@@ -140,6 +140,13 @@ SIGNATURES = {
     "ckt_update_voltages_all": (ctypes.c_int, [_P, Nodes, _P]),
     "ckt_run_loops_all": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _I32, _P]),
     "ckt_distribute_update_all": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _P]),
+    "ckt_graph_check": (ctypes.c_int, [_P, _P]),
+    "ckt_distribute_charge_all_sync": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params),
+                                                      _P]),
+    "ckt_distribute_update_all_sync": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params),
+                                                      _P]),
+    "ckt_run_loops_all_sync": (ctypes.c_int, [_P, Wires, Nodes, ctypes.POINTER(Params), _I32,
+                                              _P]),
     "ckt_graph_create": (ctypes.c_int, [ctypes.POINTER(Piece), _I32, _U32, _P, _P, _P, _P,
                                         ctypes.POINTER(_P)]),
     "ckt_graph_destroy": (ctypes.c_int, [_P]),

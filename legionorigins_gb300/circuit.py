@@ -150,12 +150,18 @@ class DeviceCircuit:
         check(L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), stream))
         check(L.ckt_update_voltages_all(g, n, stream))
 
-    def run_loops(self, prm: Params, loops: int, stream: int = 0) -> None:
+    def run_loops(self, prm: Params, loops: int, stream: int = 0, blocking: bool = False) -> None:
         """`loops` outer loops with distribute_charge and update_voltages
         fused into one node pass (two launches per loop); bit-identical to
-        `loops` calls of loop_index_space."""
-        check(lib().ckt_run_loops_all(self.graph.handle, self.wires(), self.nodes(),
-                                      ctypes.byref(prm), loops, stream))
+        `loops` calls of loop_index_space.  blocking: wait for the stream and
+        raise if a tiled node pass ran out of a copy wait (ckt_run_loops_all_sync)."""
+        fn = lib().ckt_run_loops_all_sync if blocking else lib().ckt_run_loops_all
+        check(fn(self.graph.handle, self.wires(), self.nodes(), ctypes.byref(prm), loops, stream))
+
+    def check(self, stream: int = 0) -> None:
+        """Waits for `stream` and raises CktError (CKT_ETIMEOUT) if a tiled
+        node pass on this circuit's graph left a tile unwritten."""
+        check(lib().ckt_graph_check(self.graph.handle, stream))
 
     def loop_per_piece(self, prm: Params, stream: int = 0, blocking: bool = False) -> None:
         """One outer loop as the reference's per-piece task calls: CNC for

@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     // tile's results unwritten.
     if (producer) {
       constexpr uint64_t kDrainNs = 1000000000ull;
-      atomicOr(a.error, 1u);
+      *reinterpret_cast<volatile uint32_t *>(a.error) = 1u;  // host-mapped word
+      __threadfence_system();
       mbar_wait_bounded(maskbar, 0u, kDrainNs);
       for (uint32_t n = issued > kTileStages ? issued - kTileStages : 0; n < issued; n++)
         mbar_wait_bounded(full + n % kTileStages, (n / kTileStages) & 1u, kDrainNs);

@@ -48,7 +48,7 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->tile_ent);
   cudaFree(g->tile_gw);
   cudaFree(g->tile_mask);
-  cudaFree(g->tile_error);
+  if (g->tile_error_host) cudaFreeHost(const_cast<uint32_t *>(g->tile_error_host));
   delete g;
 }
 
@@ -330,9 +330,13 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
       (rc = upload(&g->tile_steps, steps, &g->device_bytes)) ||
       (rc = upload(&g->tile_ent, all_ent, &g->device_bytes)) ||
       (rc = upload(&g->tile_gw, all_gw, &g->device_bytes)) ||
-      (rc = upload(&g->tile_mask, mask, &g->device_bytes)) ||
-      (rc = upload(&g->tile_error, std::vector<uint32_t>(1, 0u), &g->device_bytes)))
+      (rc = upload(&g->tile_mask, mask, &g->device_bytes)))
     return rc;
+  void *word = nullptr;
+  CKT_CUDA(cudaHostAlloc(&word, sizeof(uint32_t), cudaHostAllocMapped));
+  g->tile_error_host = static_cast<volatile uint32_t *>(word);
+  *g->tile_error_host = 0u;
+  CKT_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&g->tile_error), word, 0));
   g->tile_nodes = tile_nodes;
   g->num_tiles = T;
   g->tile_num_steps = (int64_t)steps.size();
@@ -455,10 +459,27 @@ int ckt_graph_tile_info(const ckt_graph *g, int32_t *tiles, int64_t *steps,
   if (stream_steps) *stream_steps = g->tile_stream_steps;
   if (error_word) {
     *error_word = 0;
-    if (g->tile_error) {
-      CKT_CUDA(cudaMemcpy(error_word, g->tile_error, 4, cudaMemcpyDeviceToHost));
-      if (*error_word) CKT_CUDA(cudaMemset(g->tile_error, 0, 4));
+    if (g->tile_error_host) {
+      // every stream's passes first: the word is then final
+      CKT_CUDA(cudaDeviceSynchronize());
+      *error_word = *g->tile_error_host;
+      *g->tile_error_host = 0u;
     }
+  }
+  return CKT_OK;
+}
+
+int ckt_graph_check(const ckt_graph *g, void *stream) {
+  CKT_REQUIRE(g != nullptr, "graph is NULL");
+  const cudaError_t e = cudaStreamSynchronize(as_stream(stream));
+  if (e != cudaSuccess)
+    return set_error(CKT_ECUDA, "waiting for the graph's passes failed: %s", cudaGetErrorString(e));
+  if (g->tile_error_host && *g->tile_error_host) {
+    *g->tile_error_host = 0u;
+    return set_error(CKT_ETIMEOUT,
+                     "a tiled node pass's copy wait ran out (bound %llu ns): a tile's charges "
+                     "and voltages were left unwritten",
+                     (unsigned long long)g->tile_timeout_ns);
   }
   return CKT_OK;
 }

@@ -146,7 +146,12 @@ struct ckt_graph {
   uint32_t *tile_gw = nullptr;     // gather steps' wire indices, parallel to their entries
   uint32_t *tile_mask = nullptr;   // [num_tiles * kTileNodesMax / 32] bit: the node's
                                    // folds are added at the end (shared/ghost, touched)
-  uint32_t *tile_error = nullptr;  // [1] bit 0: a copy wait timed out
+  // [1] bit 0: a copy wait timed out.  Pinned host memory mapped for the
+  // device: the kernel stores into tile_error, the host reads
+  // tile_error_host without a copy, so every later call on the graph sees a
+  // pass that has finished with its tile unwritten.
+  uint32_t *tile_error = nullptr;
+  volatile uint32_t *tile_error_host = nullptr;
   // Bound of the tiled pass's copy waits; a wait that runs out sets the
   // error word instead of hanging the block.
   uint64_t tile_timeout_ns = 2000000000ull;

@@ -261,6 +261,65 @@ struct DualExact {
   }
 };
 
+// EXACT, one wire per thread: DualExact's arithmetic and guards on scalar
+// instructions (the batched kernel's one-wire tiles).  Bit-identical to it.
+template <bool DTF>
+struct SoloExact {
+  float L, dt;
+  Recip kR, kC, kdt;
+  __device__ __forceinline__ SoloExact(float l, float r, float c, float d) {
+    L = l;
+    dt = d;
+    kR = make_recip(r);
+    kC = make_recip(c);
+    if (!DTF) kdt = make_recip(d);
+  }
+  static __device__ __forceinline__ bool eligible(float r, float c, float d) {
+    return divisor_ok(r, kRMin, kRMax) && divisor_ok(c, kCMin, kCMax) &&
+           (DTF || divisor_ok(d, kCMin, kCMax));
+  }
+  __device__ __forceinline__ void step(float (&ni)[10], float (&nv)[11], const float (&I0)[10],
+                                       const float (&V0)[9]) const {
+    float a1[10], a2[10];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      a1[k] = __fmul_rn(L, __fsub_rn(ni[k], I0[k]));
+      const float q1 = DTF ? dt_quot(a1[k]) : recip_quot(a1[k], kdt);
+      a2[k] = __fsub_rn(__fsub_rn(nv[k + 1], nv[k]), q1);
+      if (!DTF) bad |= outside(a1[k], kCLo, kCHi);
+      bad |= outside(a2[k], kRLo, kRHi);
+    }
+    if (!bad) {
+#pragma unroll
+      for (int k = 0; k < 10; k++) ni[k] = recip_quot(a2[k], kR);
+    } else {
+      const float R = -kR.nb;
+#pragma unroll
+      for (int k = 0; k < 10; k++)
+        ni[k] = __fdiv_rn(__fsub_rn(__fsub_rn(nv[k + 1], nv[k]), __fdiv_rn(a1[k], dt)), R);
+    }
+    float a3[9];
+    bad = DTF ? bad : false;
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      a3[k] = __fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1]));
+      if (DTF)
+        bad |= fabsf(a3[k]) < kCLo;
+      else
+        bad |= outside(a3[k], kCLo, kCHi);
+    }
+    if (!bad) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], recip_quot(a3[k], kC));
+    } else {
+      const float C = -kC.nb;
+#pragma unroll
+      for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(a3[k], C));
+    }
+  }
+};
+
 __device__ __forceinline__ const float *pick_instance(uint8_t loc, const float *pvt,
                                                       const float *shr, const float *ghost) {
   // get_node (apps/circuit/circuit_gpu.cu:40-59) without its assert: a
@@ -359,6 +418,16 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
 #pragma unroll
       for (int k = 0; k < 10; k++) ni[k] = d[k];
     }
+  } else if (MODE == CKT_MODE_EXACT && __float_as_uint(dt) == kDtBits &&
+             SoloExact<true>::eligible(a.R[w], a.C[w], dt)) {
+    const SoloExact<true> ws(a.L[w], a.R[w], a.C[w], dt);
+#pragma unroll 1
+    for (int j = 0; j < steps; j++) ws.step(ni, nv, I0, V0);
+  } else if (MODE == CKT_MODE_EXACT && __float_as_uint(dt) != kDtBits &&
+             SoloExact<false>::eligible(a.R[w], a.C[w], dt)) {
+    const SoloExact<false> ws(a.L[w], a.R[w], a.C[w], dt);
+#pragma unroll 1
+    for (int j = 0; j < steps; j++) ws.step(ni, nv, I0, V0);
   } else {
     static_assert(MODE == CKT_MODE_EXACT || MODE == CKT_MODE_EXACT_DIVIDE, "unknown mode");
     const DivideStep ws(a.L[w], a.R[w], a.C[w], dt);

@@ -13,7 +13,6 @@
 // device.
 #include <algorithm>
 #include <climits>
-#include <mutex>
 
 #include "ckt_internal.h"
 
@@ -32,26 +31,18 @@ struct NoAllocSlot {
 // its contents behind.
 static __device__ __align__(256) NoAllocSlot g_noalloc_scratch[CKT_NOALLOC_MAX_PIECES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-NoAllocSlot *g_scratch_ptr[kMaxDevices] = {};
-
-// Set-up, once per device, with that device current: the host-side name of
-// the array is not a device address, so look the address up.
+// The host-side name of the array is not a device address: look the
+// address up, with the calling thread's device current.  Looked up on every
+// call rather than cached, so a device reset or a re-created context between
+// calls cannot leave a stale address behind (the lookup is cheap once the
+// library's module is loaded on the device, which the first call does).
 int scratch_for_current_device(NoAllocSlot **out) {
-  int dev = -1;
-  CKT_CUDA(cudaGetDevice(&dev));
-  CKT_REQUIRE(dev >= 0 && dev < kMaxDevices, "device %d beyond the supported %d", dev, kMaxDevices);
-  std::lock_guard<std::mutex> g(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr)
-      return set_error(CKT_ECUDA, "cudaGetSymbolAddress of the wire-check scratch failed: %s",
-                       cudaGetErrorString(e));
-    g_scratch_ptr[dev] = static_cast<NoAllocSlot *>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr)
+    return set_error(CKT_ECUDA, "cudaGetSymbolAddress of the wire-check scratch failed: %s",
+                     cudaGetErrorString(e));
+  *out = static_cast<NoAllocSlot *>(p);
   return CKT_OK;
 }
 

@@ -150,6 +150,18 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   return CKT_OK;
 }
 
+// A tiled node pass that ran out of a copy wait left its tile's results
+// unwritten and set the graph's host-visible error word; every later
+// index-space call on the graph reports it until ckt_graph_check (or
+// ckt_graph_tile_info) clears it.
+static int check_tile_error(const ckt_graph *g) {
+  if (g->tile_error_host && *g->tile_error_host)
+    return set_error(CKT_ETIMEOUT,
+                     "an earlier tiled node pass on this graph ran out of a copy wait and left "
+                     "a tile unwritten (ckt_graph_check clears the report)");
+  return CKT_OK;
+}
+
 // Completion wait of the blocking task forms.
 static int wait_stream(void *stream, const char *task) {
   const cudaError_t e = cudaStreamSynchronize(as_stream(stream));
@@ -256,6 +268,7 @@ int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   int rc;
   CKT_REQUIRE(graph != nullptr, "graph is NULL");
   if ((rc = validate_params(prm))) return rc;
+  if ((rc = check_tile_error(graph))) return rc;
   if (graph->N == 0 || graph->W == 0) return CKT_OK;  // no wire deposits anything
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
   CKT_REQUIRE(nodes.charge != nullptr, "nodes.charge is NULL");
@@ -342,6 +355,7 @@ int ckt_distribute_update_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes
   int rc;
   CKT_REQUIRE(graph != nullptr, "graph is NULL");
   if ((rc = validate_params(prm)) || (rc = validate_nodes(nodes, "nodes"))) return rc;
+  if ((rc = check_tile_error(graph))) return rc;
   if (graph->N == 0) return CKT_OK;
   if (graph->W == 0) return ckt_update_voltages_all(graph, nodes, stream);
   if ((rc = validate_wires(wires)) || (rc = check_graph_wires(graph, wires))) return rc;
@@ -362,12 +376,31 @@ int ckt_run_loops_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
   CKT_REQUIRE(graph != nullptr, "graph is NULL");
   if ((rc = validate_params(prm)) || (rc = validate_nodes(nodes, "nodes"))) return rc;
   CKT_REQUIRE(loops >= 0, "loops must be >= 0 (got %d)", loops);
+  if ((rc = check_tile_error(graph))) return rc;
   for (int32_t l = 0; l < loops; l++) {
     if ((rc = ckt_calc_new_currents_all(graph, wires, nodes, prm, stream)) ||
         (rc = ckt_distribute_update_all(graph, wires, nodes, prm, stream)))
       return rc;
   }
   return CKT_OK;
+}
+
+int ckt_distribute_charge_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                                   const ckt_params *prm, void *stream) {
+  const int rc = ckt_distribute_charge_all(graph, wires, nodes, prm, stream);
+  return rc ? rc : ckt_graph_check(graph, stream);
+}
+
+int ckt_distribute_update_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                                   const ckt_params *prm, void *stream) {
+  const int rc = ckt_distribute_update_all(graph, wires, nodes, prm, stream);
+  return rc ? rc : ckt_graph_check(graph, stream);
+}
+
+int ckt_run_loops_all_sync(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
+                           const ckt_params *prm, int32_t loops, void *stream) {
+  const int rc = ckt_run_loops_all(graph, wires, nodes, prm, loops, stream);
+  return rc ? rc : ckt_graph_check(graph, stream);
 }
 
 int ckt_sanity_check_wires(const ckt_piece *piece, ckt_wires wires, uint32_t num_nodes_total,

@@ -219,3 +219,43 @@ def test_copy_wait_that_runs_out_reports_and_recovers(cuda, oracle):
     for k in STATE:
         assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
     assert tile_info(tiled.dc)[3] == 0
+
+
+def test_run_out_wait_is_reported_by_the_loop_calls(cuda, oracle):
+    """The loop calls do not return CKT_OK over a tile left unwritten:
+    ckt_run_loops_all_sync returns CKT_ETIMEOUT; after ckt_run_loops_all,
+    ckt_graph_check returns it, and until then every later index-space call
+    on the graph does; once checked, the same circuit runs again with the
+    oracle's bits."""
+    from legionorigins_gb300 import lib
+    from legionorigins_gb300 import circuit as C
+
+    ETIMEOUT = 4
+    c = oracle.generate(oracle.GenParams(*SHAPES["tiles_straddle_pieces"], L_offset=0.001))
+    dc = C.DeviceCircuit({k: np.ascontiguousarray(getattr(c, k)) for k in FIELDS},
+                         C.Shape(c.params.num_pieces, c.params.nodes_per_piece,
+                                 c.params.wires_per_piece))
+    assert tile_info(dc)[0] > 0
+    prm = C.params(2, 0)
+    L, g, w, n = lib(), dc.graph.handle, dc.wires(), dc.nodes()
+    assert L.ckt_graph_set_tile_timeout(g, 1) == 0
+    assert L.ckt_run_loops_all_sync(g, w, n, ctypes.byref(prm), 2, None) == ETIMEOUT
+    assert b"copy wait" in L.ckt_last_error()
+    assert L.ckt_graph_check(g, None) == 0  # the sync form already cleared it
+    assert L.ckt_run_loops_all(g, w, n, ctypes.byref(prm), 1, None) == 0  # launched
+    cuda.cuda.synchronize()
+    # a finished pass left a tile unwritten: later calls refuse to continue
+    assert L.ckt_distribute_update_all(g, w, n, ctypes.byref(prm), None) == ETIMEOUT
+    assert L.ckt_distribute_charge_all(g, w, n, ctypes.byref(prm), None) == ETIMEOUT
+    assert L.ckt_run_loops_all(g, w, n, ctypes.byref(prm), 1, None) == ETIMEOUT
+    assert L.ckt_graph_check(g, None) == ETIMEOUT
+    assert L.ckt_graph_check(g, None) == 0
+    assert L.ckt_distribute_charge_all_sync(g, w, n, ctypes.byref(prm), None) == ETIMEOUT
+    assert L.ckt_distribute_update_all_sync(g, w, n, ctypes.byref(prm), None) == ETIMEOUT
+    assert L.ckt_graph_set_tile_timeout(g, 0) == 0
+    dc.load_state({k: np.ascontiguousarray(getattr(c, k)) for k in STATE})
+    dc.run_loops(prm, 2, blocking=True)
+    got = dc.to_host()
+    oracle.simulate(c, 2, 2)
+    for k in STATE:
+        assert same_bits(got[k], getattr(c, k)), k
