@@ -186,6 +186,31 @@ def reference_sample(threads: int, target_s: float):
     return O, p, base, pieces
 
 
+def port_vs_reference() -> dict | None:
+    """The reference's own circuit.cc (compiled unmodified through the shim,
+    -O3 as its runtime.mk builds, single-threaded) timed on this host beside
+    the C restatement on one thread on the same circuit and steps: shows
+    that the restatement the CPU baseline runs is as fast as the
+    reference's own code.  None when the reference binary is not built."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ckt_oracle as O
+
+    if not os.path.exists(O.REF_BIN):
+        return None
+    p = O.GenParams(2, 1024, 4096, PCT, SEED, L_offset=0.1, L_scale=0.01)
+    try:
+        tr = min(O.time_reference(p, 1) for _ in range(2))
+    except (OSError, RuntimeError, subprocess.CalledProcessError) as e:
+        return {"unavailable": f"the reference binary did not run: {e}"}
+    tp = min(O.baseline_run(O.generate(p), 1, 10000, 1, 2) for _ in range(2))
+    return {"circuit": "2 pieces x 1024 nodes x 4096 wires/piece, 95% in-piece, the reference's "
+                       "own inductance range, 1 loop of its STEPS = 10000 inner steps",
+            "reference_s": tr, "port_s": tp, "port_over_reference_rate": tr / tp,
+            "note": "apps/circuit/circuit.cc's own main loop (its ELAPSED TIME), built "
+                    "unmodified through oracle/refshim at -O3, single-threaded; the port "
+                    "(oracle/ckt_oracle.c) on one thread"}
+
+
 def run_reference_arm(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -229,7 +254,8 @@ def run_reference_arm(args) -> None:
         "data": "synthetic (reference generator, seed 12345)",
         "config": workload_config("reference CPU tasks (IEEE fp32)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample,
+                         "port_vs_reference_single_thread": port_vs_reference()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -604,7 +630,8 @@ def main() -> None:
             "cores": threads, "kind": "port",
             "sample": f"1 outer loop x {INNER_STEPS} inner steps over {pieces} of {p.num_pieces} "
                       f"pieces ({pieces * p.wires_per_piece} wires), reference CPU tasks "
-                      f"restated in C (oracle/ckt_oracle.c), {threads} threads",
+                      f"restated in C (oracle/ckt_oracle.c, -O3), {threads} threads",
+            "port_vs_reference_single_thread": port_vs_reference(),
         }
 
     # Accuracy of the arithmetic this run uses, stated with the number (the

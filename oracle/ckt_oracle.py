@@ -51,13 +51,41 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(reference: str = "/root/reference") -> str | None:
-    """Compile the reference's circuit.cc through the shim when the reference
-    tree is present (only in the development container)."""
-    if not os.path.isdir(os.path.join(reference, "apps", "circuit")):
+STAGED_REFERENCE = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "LegionOrigins")
+
+
+def build_ref(reference: str | None = None) -> str | None:
+    """Compile the reference's circuit.cc (and reducetest.cc) through the
+    shim: from the reference tree when it is present (and stage the files
+    those builds read into the git-ignored baseline/_ref/LegionOrigins), else
+    from that staged copy; None when neither exists."""
+    if reference and os.path.isdir(os.path.join(reference, "apps", "circuit")):
+        subprocess.run(["make", "-s", "-C", HERE, "stage", f"REFERENCE={reference}",
+                        f"STAGE={STAGED_REFERENCE}"], check=True)
+    elif os.path.isdir(os.path.join(STAGED_REFERENCE, "apps", "circuit")):
+        reference = STAGED_REFERENCE
+    else:
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference}"], check=True)
     return REF_BIN
+
+
+def time_reference(p: "GenParams", loops: int = 1) -> float:
+    """ELAPSED TIME of the reference's own circuit.cc main loop
+    (apps/circuit/circuit.cc:311-318: `loops` outer loops of STEPS = 10000
+    inner steps, its CPU tasks, single-threaded through the shim), seconds."""
+    if not os.path.exists(REF_BIN):
+        raise FileNotFoundError(REF_BIN)
+    if p.L_offset != 0.1 or p.L_scale != 0.01:
+        raise ValueError("the reference hard-codes L = drand48()*0.01 + 0.1")
+    args = [REF_BIN, "-l", str(loops), "-p", str(p.num_pieces), "-npp", str(p.nodes_per_piece),
+            "-wpp", str(p.wires_per_piece), "-pct", str(int(p.pct_wire_in_piece)),
+            "-s", str(p.random_seed)]
+    out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
+    for line in out.splitlines():
+        if line.startswith("ELAPSED TIME"):
+            return float(line.split("=")[1].split()[0])
+    raise RuntimeError("the reference printed no ELAPSED TIME")
 
 
 _lib = None
