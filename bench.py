@@ -549,7 +549,7 @@ def main() -> None:
     ap.add_argument("--no-extras", action="store_true",
                     help="plain workload: skip the config-0/config-2, finite-regime, FAST, "
                          "batched and served sub-measurements")
-    ap.add_argument("--extra-serve-rates", default="60,120",
+    ap.add_argument("--extra-serve-rates", default="120,260",
                     help="plain workload: offered request rates (requests/s) of the served "
                          "sub-measurement")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
@@ -574,6 +574,9 @@ def main() -> None:
                          "(default: the library's)")
     ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
                     help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
+    ap.add_argument("--batch-launch", default="",
+                    help="batched, profiling only: launch shape block,wires_per_thread,dc_schedule "
+                         "instead of the autotuner's choice")
     ap.add_argument("--circuits", type=int, default=256,
                     help="batched: number of circuits of the mix (256 for the benchmark; fewer "
                          "only to profile)")
@@ -1014,7 +1017,11 @@ def batched_result(args, torch, G, ws, local, dist, mode, steps, warmup, piece_s
     info = b.info()
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    cfg = b.autotune(mode, sp)
+    if getattr(args, "batch_launch", ""):
+        b.set_config(*(int(x) for x in args.batch_launch.split(",")))
+        cfg = b.config()
+    else:
+        cfg = b.autotune(mode, sp)
     updates = info["segment_updates_per_run"]
     E = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 

@@ -168,6 +168,24 @@ int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires
                           ckt_nodes pvt, float *shr_fold, float *ghost_fold,
                           const ckt_params *prm, void *stream);
 
+/* Replaces distribute_charge_gpu (apps/circuit/circuit.h:90-95,
+ * apps/circuit/circuit_gpu.cu:219-304) with the reference's own arguments:
+ * the piece and its instances, no contribution graph.  Each wire of the
+ * piece adds -dt*I[0] to its in-node and +dt*I[9] to its out-node with
+ * atomic adds: private nodes' charge in `pvt` directly (apply), shared and
+ * ghost nodes into `shr_fold` / `ghost_fold` (fold; float per absolute node
+ * index, holding the identity 0 on entry as a fresh reduction instance
+ * does).  Lanes of a warp whose ends land on the same node combine their
+ * contributions first, so a heavily shared node takes one atomic per warp.
+ * Like the reference's atomicAdd, the order of the additions at a node is
+ * unspecified: sums may differ in the last bits from run to run and from the
+ * deterministic ckt_distribute_charge.  Wires must pass
+ * ckt_sanity_check_wires (locations in {0,1,2}, pointers inside their
+ * instances); nothing else is checked on the device. */
+int ckt_distribute_charge_atomic(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                                 float *shr_fold, float *ghost_fold, const ckt_params *prm,
+                                 void *stream);
+
 /* The runtime's application of piece `piece_index`'s reduction instances
  * (runtime/lowlevel_dma.cc:323-355): charge[x] += fold[x] for every shared
  * or ghost node the piece touched, then fold[x] = 0.  Call pieces in
@@ -195,6 +213,9 @@ int ckt_distribute_charge_sync(const ckt_graph *graph, int32_t piece_index, ckt_
                                const ckt_params *prm, void *stream);
 int ckt_update_voltages_sync(const ckt_piece *piece, ckt_nodes pvt, ckt_nodes shr,
                              const int32_t *locator, void *stream);
+int ckt_distribute_charge_atomic_sync(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                                      float *shr_fold, float *ghost_fold, const ckt_params *prm,
+                                      void *stream);
 
 /* Replaces sanity_check_wires_gpu (apps/circuit/circuit.h:103-104,
  * apps/circuit/circuit_gpu.cu:151-217) without its asserts: validates every
@@ -502,8 +523,8 @@ typedef struct {
   double busy_s, clock_s;
 } ckt_server_stats;
 
-/* 80 GB budget, 4096 slots, one prep thread per host core, FAST, results
- * not kept, 5 s round timeout, launch {256, 1, 2}, device generation. */
+/* 80 GB budget, 4096 slots, one prep thread per host core, EXACT, results
+ * not kept, 5 s round timeout, launch {128, 2, 0}, device generation. */
 void ckt_server_default_config(ckt_server_config *config);
 int ckt_server_create(const ckt_server_config *config, ckt_server **out);
 /* Non-blocking; the id must be unused among the server's open requests. */

@@ -127,6 +127,10 @@ SIGNATURES = {
     "ckt_distribute_charge": (ctypes.c_int, [_P, _I32, Wires, Nodes, _P, _P,
                                              ctypes.POINTER(Params), _P]),
     "ckt_apply_fold": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P]),
+    "ckt_distribute_charge_atomic": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, Nodes, _P, _P,
+                                                    ctypes.POINTER(Params), _P]),
+    "ckt_distribute_charge_atomic_sync": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, Nodes,
+                                                         _P, _P, ctypes.POINTER(Params), _P]),
     "ckt_update_voltages": (ctypes.c_int, [ctypes.POINTER(Piece), Nodes, Nodes, _P, _P]),
     "ckt_calc_new_currents_sync": (ctypes.c_int, [ctypes.POINTER(Piece), Wires, Nodes, Nodes,
                                                   Nodes, ctypes.POINTER(Params), _P]),

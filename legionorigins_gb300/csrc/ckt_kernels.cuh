@@ -730,6 +730,53 @@ static __global__ void __launch_bounds__(256)
   tgt[x] = acc;
 }
 
+// One piece without the contribution graph (distribute_charge_kernel,
+// apps/circuit/circuit_gpu.cu:245-286): one thread per wire adds -dt*I[0]
+// to its in-node and dt*I[9] to its out-node with atomic adds -- private
+// nodes into pvt's charge, shared and ghost nodes into their fold instances
+// (reduce_local, circuit_gpu.cu:219-243).  Lanes of a warp whose wire ends
+// land on the same node of the same instance first combine their
+// contributions: __match_any_sync groups them, and the group's first lane
+// adds the group's sum, in lane order, with one atomic.  The order of the
+// additions at a node is unspecified, as with the reference's atomicAdd.
+__device__ __forceinline__ void warp_aggregated_add(float *target, float v, uint64_t key,
+                                                    float *sbuf) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t peers = __match_any_sync(__activemask(), key);
+  if (peers == (1u << lane)) {
+    atomicAdd(target, v);
+    return;
+  }
+  sbuf[lane] = v;
+  __syncwarp(peers);
+  if (lane == (uint32_t)(__ffs(peers) - 1)) {
+    float sum = sbuf[lane];
+    for (uint32_t m = peers & (peers - 1); m; m &= m - 1) sum = __fadd_rn(sum, sbuf[__ffs(m) - 1]);
+    atomicAdd(target, sum);
+  }
+  __syncwarp(peers);  // sbuf is reused by the wire's other end
+}
+
+static __global__ void __launch_bounds__(256)
+    dc_atomic_kernel(uint32_t first_wire, uint32_t num_wires, const uint32_t *__restrict__ in_ptr,
+                     const uint32_t *__restrict__ out_ptr, const uint8_t *__restrict__ in_loc,
+                     const uint8_t *__restrict__ out_loc, const float *__restrict__ I0,
+                     const float *__restrict__ I9, float *pvt_charge, float *shr_fold,
+                     float *ghost_fold, float dt) {
+  __shared__ float sbuf[256];
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= num_wires) return;
+  const uint32_t w = first_wire + t;
+  float *warp_buf = sbuf + (threadIdx.x & ~31u);
+  const uint32_t a = in_ptr[w], b = out_ptr[w];
+  const uint8_t la = in_loc[w], lb = out_loc[w];
+  const float ca = __fmul_rn(-dt, I0[w]), cb = __fmul_rn(dt, I9[w]);
+  float *ta = la == CKT_PRIVATE_PTR ? pvt_charge : (la == CKT_SHARED_PTR ? shr_fold : ghost_fold);
+  float *tb = lb == CKT_PRIVATE_PTR ? pvt_charge : (lb == CKT_SHARED_PTR ? shr_fold : ghost_fold);
+  warp_aggregated_add(ta + a, ca, ((uint64_t)(la > 2 ? 2 : la) << 32) | a, warp_buf);
+  warp_aggregated_add(tb + b, cb, ((uint64_t)(lb > 2 ? 2 : lb) << 32) | b, warp_buf);
+}
+
 // Application of one piece's reduction instances.
 static __global__ void __launch_bounds__(256)
     apply_fold_kernel(uint32_t t0, uint32_t nt, const uint32_t *__restrict__ touch_node,

@@ -572,12 +572,12 @@ void ckt_server_default_config(ckt_server_config *c) {
   c->hbm_budget_bytes = 80ull << 30;
   c->max_circuits = 4096;
   c->prep_threads = (int32_t)std::max(1u, std::thread::hardware_concurrency());
-  c->mode = CKT_MODE_FAST;
+  c->mode = CKT_MODE_EXACT;
   c->keep_results = 0;
   c->round_timeout_ns = 5000000000ull;
-  c->launch.block = 256;
-  c->launch.wires_per_thread = 1;
-  c->launch.dc_schedule = 2;
+  c->launch.block = 128;
+  c->launch.wires_per_thread = 2;
+  c->launch.dc_schedule = 0;
   c->device_generate = 1;
 }
 

@@ -248,6 +248,39 @@ int ckt_distribute_charge(const ckt_graph *graph, int32_t piece_index, ckt_wires
   return CKT_OK;
 }
 
+int ckt_distribute_charge_atomic(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                                 float *shr_fold, float *ghost_fold, const ckt_params *prm,
+                                 void *stream) {
+  CKT_REQUIRE(piece != nullptr, "piece is NULL");
+  int rc;
+  if ((rc = validate_params(prm))) return rc;
+  if (piece->num_wires == 0) return CKT_OK;
+  CKT_REQUIRE(wires.in_ptr && wires.out_ptr && wires.in_loc && wires.out_loc,
+              "wire pointer/location arrays are NULL");
+  CKT_REQUIRE(wires.current != nullptr && wires.seg_stride > 0,
+              "wire currents are NULL or seg_stride is not positive");
+  CKT_REQUIRE((int64_t)piece->first_wire + piece->num_wires <= wires.seg_stride,
+              "wire range [%u, %llu) exceeds seg_stride %lld", piece->first_wire,
+              (unsigned long long)piece->first_wire + piece->num_wires,
+              (long long)wires.seg_stride);
+  CKT_REQUIRE(pvt.charge != nullptr && shr_fold != nullptr && ghost_fold != nullptr,
+              "pvt.charge or a fold instance is NULL");
+  const float *I0 = wires.current, *I9 = wires.current + 9 * wires.seg_stride;
+  dc_atomic_kernel<<<grid_for(piece->num_wires), 256, 0, as_stream(stream)>>>(
+      piece->first_wire, piece->num_wires, wires.in_ptr, wires.out_ptr, wires.in_loc,
+      wires.out_loc, I0, I9, pvt.charge, shr_fold, ghost_fold, prm->dt);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+int ckt_distribute_charge_atomic_sync(const ckt_piece *piece, ckt_wires wires, ckt_nodes pvt,
+                                      float *shr_fold, float *ghost_fold, const ckt_params *prm,
+                                      void *stream) {
+  const int rc =
+      ckt_distribute_charge_atomic(piece, wires, pvt, shr_fold, ghost_fold, prm, stream);
+  return rc ? rc : wait_stream(stream, "distribute_charge");
+}
+
 int ckt_apply_fold(const ckt_graph *graph, int32_t piece_index, float *shr_fold, float *ghost_fold,
                    float *charge, void *stream) {
   CKT_REQUIRE(graph != nullptr, "graph is NULL");

@@ -13,7 +13,7 @@ from .workloads import CircuitSpec
 
 
 class Server:
-    def __init__(self, mode: int = 1, hbm_budget_bytes: int = 80 << 30, max_circuits: int = 4096,
+    def __init__(self, mode: int = 0, hbm_budget_bytes: int = 80 << 30, max_circuits: int = 4096,
                  prep_threads: int = 0, keep_results: bool = False, launch=None,
                  round_timeout_ns: int = 0, device_generate: bool = True):
         cfg = ServerConfig()

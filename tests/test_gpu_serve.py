@@ -32,13 +32,14 @@ def alone(cuda, s, mode):
 
 
 @pytest.mark.parametrize("device_generate", [True, False])
-def test_each_result_is_the_same_alone_and_in_the_mix(cuda, device_generate):
+@pytest.mark.parametrize("mode", [0, 1], ids=["exact", "fast"])
+def test_each_result_is_the_same_alone_and_in_the_mix(cuda, device_generate, mode):
     from legionorigins_gb300.serve import Server
 
     mix = [spec(8, 64, 256, 101, 40, 3), spec(12, 30, 120, 102, 25, 1),
            spec(20, 256, 1024, 103, 60, 2), spec(9, 5, 20, 104, 33, 5),
            spec(64, 128, 512, 105, 10, 4), spec(16, 1000, 4000, 106, 15, 2)]
-    srv = Server(mode=1, keep_results=True, prep_threads=4, device_generate=device_generate)
+    srv = Server(mode=mode, keep_results=True, prep_threads=4, device_generate=device_generate)
     # staggered arrivals: later requests arrive while earlier ones run
     for i, s in enumerate(mix):
         srv.submit(i, s)
@@ -51,7 +52,7 @@ def test_each_result_is_the_same_alone_and_in_the_mix(cuda, device_generate):
     assert st["rounds"] >= max(s.loops for s in mix)
     for i, s in enumerate(mix):
         got = srv.take_result(i)
-        ref = alone(cuda, s, 1)
+        ref = alone(cuda, s, mode)
         for k in STATE:
             assert np.array_equal(got[k].view(np.uint32), ref[k].view(np.uint32)), (i, k)
     srv.close()
