@@ -73,6 +73,10 @@ CNC_TRAFFIC_PER_WIRE = (103.879424e6 + 21.284608e6) / 1048576  # measured DRAM b
 
 
 def workload_config(mode: str, pieces: int = SHAPE["num_pieces"]) -> dict:
+    if INNER_STEPS != 1000:
+        return {"workload": "PROFILING CASE, not the configured workload: the heavy-reduction "
+                            "circuit (128 x 8192 x 32768, 50% in-piece, S=500 x 10 loops)",
+                "mode": mode}
     if pieces != SHAPE["num_pieces"]:
         return {"workload": f"PROFILING CASE, not the configured workload: {pieces} pieces x "
                             f"16384 nodes x 65536 wires/piece, S=1000 x 10 loops", "mode": mode}
@@ -539,6 +543,7 @@ def plain_measure(torch, G, C, host, shape, mode, inner, loops, steps, warmup, l
 
 
 def main() -> None:
+    global INNER_STEPS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -572,6 +577,9 @@ def main() -> None:
     ap.add_argument("--serve-launch", default="",
                     help="serve: round launch shape block,wires_per_thread,dc_schedule "
                          "(default: the library's)")
+    ap.add_argument("--plain-config", type=int, choices=[1, 2], default=1,
+                    help="profiling only: 2 times the heavy-reduction circuit (128 x 8192 x "
+                         "32768, 50%% in-piece, S=500) as the plain workload instead of config 1")
     ap.add_argument("--pieces", type=int, default=SHAPE["num_pieces"],
                     help="profiling only: simulate the first P pieces' shape (P x 16384 x 65536)")
     ap.add_argument("--batch-launch", default="",
@@ -645,9 +653,14 @@ def main() -> None:
         accuracy = accuracy_check(torch, G, C, mode, (SHAPE["num_pieces"], SHAPE["nodes_per_piece"],
                                                       SHAPE["wires_per_piece"], PCT), INNER_STEPS)
 
-    shape = C.Shape(args.pieces, SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"])
-    host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
-                      SEED + 0, L_OFFSET, L_SCALE)
+    if args.plain_config == 2:  # profiling: the heavy-reduction circuit as the plain workload
+        INNER_STEPS = 500
+        shape = C.Shape(128, 8192, 32768)
+        host = C.generate(128, 8192, 32768, 50.0, SEED, L_OFFSET, L_SCALE)
+    else:
+        shape = C.Shape(args.pieces, SHAPE["nodes_per_piece"], SHAPE["wires_per_piece"])
+        host = C.generate(shape.num_pieces, shape.nodes_per_piece, shape.wires_per_piece, PCT,
+                          SEED + 0, L_OFFSET, L_SCALE)
     dc = C.DeviceCircuit(host, shape, device=f"cuda:{local}")
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream

@@ -599,8 +599,12 @@ int ckt_server_create(const ckt_server_config *cfg, ckt_server **out) {
   if ((rc = round_blocks_per_sm(s->cfg.launch, &per_sm))) return rc;
   s->cfg.launch.blocks_per_sm = per_sm;
   s->grid = s->sm_count * per_sm;
-  CKT_CUDA(cudaStreamCreateWithFlags(&s->compute, cudaStreamNonBlocking));
-  CKT_CUDA(cudaStreamCreateWithFlags(&s->io, cudaStreamNonBlocking));
+  // Rounds outrank circuit building and copies: when a round ends, the next
+  // round's blocks are dispatched before the generator's and the copies'.
+  int least = 0, greatest = 0;
+  CKT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  CKT_CUDA(cudaStreamCreateWithPriority(&s->compute, cudaStreamNonBlocking, greatest));
+  CKT_CUDA(cudaStreamCreateWithPriority(&s->io, cudaStreamNonBlocking, least));
   for (auto &st : s->stage) {
     CKT_CUDA(cudaEventCreate(&st.start));
     CKT_CUDA(cudaEventCreate(&st.end));
