@@ -152,3 +152,25 @@ def test_full_size_finite_regime_exact(cuda, oracle, cfg):
         print(f"{cfg} {k}: EXACT vs fp64 max {r64.max():.2e} rms {np.sqrt((r64 ** 2).mean()):.2e}; "
               f"FAST vs fp32 reference max {rf.max():.2e} (elements over 1e-5: "
               f"{int((rf > 1e-5).sum())} of {rf.size})")
+
+
+@pytest.mark.parametrize("steps", [16, 17, 100])
+def test_exact_all_nan_wires_beside_finite_ones(cuda, oracle, steps):
+    """Wires whose whole state is NaN drop the quotient guards (no dividend
+    can then leave NaN); their neighbours in the same warps keep them.  Both
+    end with the divide-routine form's bits and the oracle's."""
+    c = oracle.generate(oracle.GenParams(4, 256, 1024, 95, 21, L_offset=0.001))
+    rng = np.random.default_rng(steps)
+    c.current[:] = rng.uniform(-1, 1, c.current.shape).astype(np.float32)
+    c.voltage[:] = rng.uniform(-1, 1, c.voltage.shape).astype(np.float32)
+    nan_wires = rng.random(c.current.shape[1]) < 0.5
+    c.current[:, nan_wires] = np.nan
+    c.voltage[:, nan_wires] = np.nan
+    a = cnc(cuda, device(c), steps, EXACT)
+    b = cnc(cuda, device(c), steps, EXACT_DIVIDE)
+    for k in ("current", "voltage"):
+        assert same_bits(a[k], b[k]), k
+        assert np.isnan(a[k][:, nan_wires]).all(), k
+    oracle.calc_new_currents(c, steps)
+    for k in ("current", "voltage"):
+        assert same_bits(a[k], getattr(c, k)), k
