@@ -9,9 +9,14 @@
 // the graph, encoding in ckt_internal.h): for a chunk holding many of them,
 // one lane of a copy warp moves the chunk's I[0] and I[9] slices and the
 // step's entry block into a three-stage shared-memory ring with cp.async.bulk
-// (completion on the stage's mbarrier); the few contributions of sparse
-// chunks are gathered from global memory through staged wire indices.  31
-// consumer warps own disjoint node sets, so they walk the steps without
+// (completion on the stage's mbarrier).  The few contributions of sparse
+// chunks -- in the benchmark circuits, the wires that end in another piece
+// -- are packed first by ghost_pack_kernel, which reads their currents in
+// wire order and stores each into its step's run of the graph's ghost
+// buffer; the copy warp moves those runs like a chunk's slices.  (Gathering
+// them inside the tile pass read one random 32-byte sector per value, mostly
+// from DRAM, since the streamed chunks keep evicting the currents from L2.)
+// 31 consumer warps own disjoint node sets, so they walk the steps without
 // block barriers and hand each stage back through a second mbarrier; each
 // lane sums its own list of whole node runs, balanced within the warp.  Each
 // node still adds its contributions in CSR order -- private nodes in place,
@@ -106,8 +111,9 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 
 constexpr uint32_t kTileBlock = 32 * (kTileWarps + 1);  // consumer warps + one copy warp
 constexpr uint32_t kTileStages = 3;
-// Shared memory of one stage: I[0] and I[9] slices of a chunk (a gather
-// step's wire indices instead), then the step's block (header + entries).
+// Shared memory of one stage: I[0] and I[9] slices of a chunk (a ghost
+// step's in-end and out-end runs in their place), then the step's block
+// (header + entries).
 constexpr uint32_t kStageVals = 2 * kChunkWires;
 constexpr uint32_t kStageBlockWords = kStepHeaderWords + kStepEntriesMax;
 constexpr uint32_t kStageBytes = (kStageVals + kStageBlockWords) * 4;
@@ -115,7 +121,8 @@ constexpr uint32_t kStageBytes = (kStageVals + kStageBlockWords) * 4;
 struct DcTileArgs {
   const uint32_t *tile_step;
   const uint4 *steps;
-  const uint32_t *ent, *gw;
+  const uint32_t *ent;
+  const float *ghost;  // ghost steps' values, packed by ghost_pack_kernel
   const uint32_t *mask;  // per tile: nodes whose folds are added at the end
   const float *I0, *I9;  // 16-byte aligned; slices may be read up to a multiple of 4 wires
   float *charge, *voltage;
@@ -158,27 +165,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 // One lane sums its list of node runs in a step: entries [b, e) of the
-// step's block, runs back to back, each opened by a head entry.  Stream
-// steps read currents from the staged chunk slices, gather steps from global
-// memory at the staged wire indices.
+// step's block, runs back to back, each opened by a head entry; an entry's
+// current is svals[end * kChunkWires + index].
 __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const float *svals,
-                                                  uint32_t b, uint32_t e, bool stream,
-                                                  const float *__restrict__ I0,
-                                                  const float *__restrict__ I9, float *sacc,
+                                                  uint32_t b, uint32_t e, float *sacc,
                                                   float *sfold, float dt) {
-  const uint32_t *sgw = reinterpret_cast<const uint32_t *>(svals);
   uint32_t node = 0xffffffffu;
   float acc = 0.0f, fold = 0.0f;
   for (uint32_t p = b; p < e; p++) {
     const uint32_t u = sent[p];
     const uint32_t end = (u & kTeEnd) ? 1u : 0u;
-    float v;
-    if (stream) {
-      v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
-    } else {
-      const uint32_t w = sgw[p];
-      v = end ? I9[w] : I0[w];
-    }
+    const float v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
     if (u & kTeHead) {
       if (node != 0xffffffffu) {
         sacc[node] = acc;
@@ -202,6 +199,89 @@ __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const fl
   if (node != 0xffffffffu) {
     sacc[node] = acc;
     sfold[node] = fold;
+  }
+}
+
+// Programmatic dependent launch: the tile pass is launched to start while
+// ghost_pack_kernel still runs, and its copy lane waits for the packing's
+// end (and the visibility of its stores) before the first ghost step's copy.
+__device__ __forceinline__ void grid_dependents_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Fills the ghost buffer: ghost[slot] = I[end][wire] for each list entry.
+// The list is sorted by source block of kPackWires wires, then by slot.
+//  * Many ghost ends (STAGED): a block takes one source block: it loads the
+//    block's I[0] and/or I[9] slices into shared memory with coalesced
+//    loads, then stores the block's entries from there, so that the stores
+//    into one step's run go out together.  Its first kPackPer entries per
+//    thread are loaded before the slices, so that the two loads overlap.
+//  * Few ghost ends (whole slices would be mostly unused): a thread takes
+//    kPackPer entries spread over the list and reads each current directly,
+//    all its loads in flight together.
+// Either way the tile pass may already be running (programmatic dependent
+// launch); it waits for this grid before its first ghost step's copy.
+constexpr uint32_t kPackBlock = 512, kPackPer = 4;
+template <bool STAGED>
+__global__ void __launch_bounds__(kPackBlock, 3) ghost_pack_kernel(const uint2 *__restrict__ list,
+                                                                   const uint32_t *__restrict__ blk,
+                                                                   uint32_t n, uint32_t W,
+                                                                   const float *__restrict__ I0,
+                                                                   const float *__restrict__ I9,
+                                                                   float *__restrict__ ghost) {
+  __shared__ float4 sv[STAGED ? 2 * kPackWires / 4 : 1];
+  grid_dependents_launch();
+  uint32_t first, last, stride, w0 = 0, d = 0;
+  if (STAGED) {
+    d = blk[blockIdx.x];
+    first = (d & kPackFirstMask) + threadIdx.x;
+    last = blk[blockIdx.x + 1] & kPackFirstMask;
+    if (first - threadIdx.x == last) return;
+    stride = kPackBlock;
+    w0 = blockIdx.x * kPackWires;
+  } else {
+    first = blockIdx.x * kPackBlock + threadIdx.x;
+    last = n;
+    stride = gridDim.x * kPackBlock;
+  }
+  uint2 e[kPackPer];
+#pragma unroll
+  for (uint32_t j = 0; j < kPackPer; j++) {
+    const uint32_t k = first + j * stride;
+    e[j] = k < last ? list[k] : make_uint2(0xffffffffu, 0u);
+  }
+  if (STAGED) {
+    const uint32_t nw4 = (min(kPackWires, W - w0) + 3u) / 4u;  // arrays extend to a multiple of 4
+    const float4 *src0 = reinterpret_cast<const float4 *>(I0 + w0);
+    const float4 *src1 = reinterpret_cast<const float4 *>(I9 + w0);
+    for (uint32_t i = threadIdx.x; i < nw4; i += kPackBlock) {
+      if (d & kPackHasIn) sv[i] = __ldcs(src0 + i);
+      if (d & kPackHasOut) sv[kPackWires / 4 + i] = __ldcs(src1 + i);
+    }
+    __syncthreads();
+    const float *sf = reinterpret_cast<const float *>(sv);
+#pragma unroll
+    for (uint32_t j = 0; j < kPackPer; j++)
+      if (e[j].x != 0xffffffffu)
+        ghost[e[j].x] = sf[(e[j].y & 1u) * kPackWires + (e[j].y >> 1) - w0];
+    for (uint32_t k = first + kPackPer * stride; k < last; k += stride) {
+      const uint2 f = list[k];
+      ghost[f.x] = sf[(f.y & 1u) * kPackWires + (f.y >> 1) - w0];
+    }
+  } else {
+    float v[kPackPer];
+#pragma unroll
+    for (uint32_t j = 0; j < kPackPer; j++)
+      if (e[j].x != 0xffffffffu) v[j] = (e[j].y & 1u) ? I9[e[j].y >> 1] : I0[e[j].y >> 1];
+#pragma unroll
+    for (uint32_t j = 0; j < kPackPer; j++)
+      if (e[j].x != 0xffffffffu) ghost[e[j].x] = v[j];
   }
 }
 
@@ -251,31 +331,38 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   // Copy warp: the copies of step s into its stage (after the stage's
   // previous contents have been handed back).
   uint32_t issued = 0;
+  bool packed = false;  // the ghost buffer is known to be filled
   auto issue = [&](uint32_t s) -> bool {
     const uint32_t n = s - s0, slot = n % kTileStages;
     if (n >= kTileStages &&
         !mbar_wait_abortable(empty + slot, ((n / kTileStages) - 1) & 1u, abort, a.timeout_ns))
       return false;
     const uint4 st = a.steps[s];
-    const uint32_t nent = st.y - kStepHeaderWords;
-    uint32_t bytes = st.y * 4, nw = 0;
-    if (st.z != kGatherStep) {
-      nw = (min(kChunkWires, a.W - st.z * kChunkWires) + 3u) & ~3u;
-      bytes += 2 * nw * 4;
+    if ((st.z & kGhostStep) != 0u && !packed) {
+      grid_dependency_wait();
+      fence_proxy_async_global();
+      packed = true;
+    }
+    // in-end and out-end values: [0, n0) and [kChunkWires, kChunkWires + n1)
+    const float *src0, *src1;
+    uint32_t n0, n1;
+    if ((st.z & kGhostStep) == 0u) {
+      n0 = n1 = (min(kChunkWires, a.W - st.z * kChunkWires) + 3u) & ~3u;
+      src0 = a.I0 + st.z * kChunkWires;
+      src1 = a.I9 + st.z * kChunkWires;
     } else {
-      bytes += nent * 4;
+      n0 = (((st.z >> kGhostCountBits) & kGhostCountMask) + 3u) & ~3u;
+      n1 = ((st.z & kGhostCountMask) + 3u) & ~3u;
+      src0 = a.ghost + st.w;
+      src1 = src0 + n0;
     }
     uint64_t *bar = full + slot;
     fence_proxy_async_smem();
-    mbar_expect_tx(bar, bytes);
-    if (st.z != kGatherStep) {
-      bulk_g2s(vals_of(slot), a.I0 + st.z * kChunkWires, nw * 4, bar);
-      bulk_g2s(vals_of(slot) + kChunkWires, a.I9 + st.z * kChunkWires, nw * 4, bar);
-    } else if (nent > 0) {
-      bulk_g2s(vals_of(slot), a.gw + st.w, nent * 4, bar);
-    }
+    mbar_expect_tx(bar, (st.y + n0 + n1) * 4);
+    if (n0) bulk_g2s(vals_of(slot), src0, n0 * 4, bar);
+    if (n1) bulk_g2s(vals_of(slot) + kChunkWires, src1, n1 * 4, bar);
     bulk_g2s(block_of(slot), a.ent + st.x, st.y * 4, bar);
-    issued = n + 1;
+    issued = max(issued, n + 1);
     return true;
   };
   const bool producer = warp == kTileWarps && lane == 0;
@@ -284,7 +371,11 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     fence_proxy_async_smem();
     mbar_expect_tx(maskbar, kMaskWords * 4);
     bulk_g2s(smask, a.mask + (size_t)t * kMaskWords, kMaskWords * 4, maskbar);
-    for (; s_next < min(s1, s0 + kTileStages); s_next++) issue(s_next);
+    // The first stages' copies; a ghost step among them waits for the
+    // packing, after the barrier below (each of these stages is used for the
+    // first time, so the others go ahead out of order).
+    for (; s_next < min(s1, s0 + kTileStages); s_next++)
+      if ((a.steps[s_next].z & kGhostStep) == 0u) issue(s_next);
   }
   // Node data staged for the last pass: elements [0, nn4) of each array.
   const uint32_t nn4 = nn & ~3u, nsteps = s1 - s0;
@@ -316,6 +407,8 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   bool node_issued = false;
   if (warp == kTileWarps) {
     if (producer) {
+      for (uint32_t s = s0; s < min(s1, s0 + kTileStages); s++)
+        if ((a.steps[s].z & kGhostStep) != 0u) issue(s);  // never waits: a first use
       for (; s_next < s1; s_next++)
         if (!issue(s_next)) {
           *abort = 1u;
@@ -357,9 +450,8 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       const uint16_t *hdr = reinterpret_cast<const uint16_t *>(blk);
       const uint32_t last = hdr[kTileLanes];
       const uint32_t l = threadIdx.x;  // consumer lane list (warp * 32 + lane)
-      const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : last & ~kStepGatherFlag;
-      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e,
-                        (last & kStepGatherFlag) == 0u, a.I0, a.I9, sacc, sfold, a.dt);
+      const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : last;
+      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e, sacc, sfold, a.dt);
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + slot);
     }

@@ -46,8 +46,11 @@ static void free_graph(ckt_graph *g) {
   cudaFree(g->tile_step);
   cudaFree(g->tile_steps);
   cudaFree(g->tile_ent);
-  cudaFree(g->tile_gw);
   cudaFree(g->tile_mask);
+  cudaFree(g->ghost);
+  cudaFree(g->ghost_list);
+  cudaFree(g->ghost_block);
+  if (g->ghost_done) cudaEventDestroy(g->ghost_done);
   if (g->tile_error_host) cudaFreeHost(const_cast<uint32_t *>(g->tile_error_host));
   delete g;
 }
@@ -151,13 +154,15 @@ int build_node_csr(const ckt_piece *pieces, int32_t num_pieces, uint32_t num_nod
 namespace {
 
 struct TilePlan {
-  std::vector<uint4> steps;  // entry and gather-wire offsets local to the tile
-  std::vector<uint32_t> ent, gw;
+  std::vector<uint4> steps;  // entry and ghost-slot offsets local to the tile
+  std::vector<uint32_t> ent;
+  std::vector<uint32_t> gsrc;  // per ghost slot: wire << 1 | end, or kTePad
 };
 
 // A chunk with at least this many of the tile's contributions is copied
-// whole (16 KB of I[0]/I[9]); sparser chunks are gathered entry by entry,
-// each gather costing a 32-byte sector.
+// whole (32 KB of I[0]/I[9]); the contributions of sparser chunks go
+// through the ghost buffer (a list entry, a current read in wire order, a
+// scattered store and a copy: about 20 bytes and one store request each).
 constexpr uint32_t kDenseMin = kChunkWires / 8;
 
 void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t xe,
@@ -194,8 +199,9 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
   std::vector<uint32_t> order;
   std::vector<std::pair<uint32_t, uint32_t>> wruns[kTileWarps];
   std::vector<uint32_t> lane_runs[32];
-  auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, uint32_t chunk) {
-    const bool gather = chunk == kGatherStep;
+  std::vector<uint32_t> gidx, gin, gout;
+  auto emit = [&](const std::vector<uint64_t> &v, size_t a, size_t b, bool ghost,
+                  uint32_t chunk) {
     runs.clear();
     for (size_t j = a; j < b;) {
       const uint64_t node = v[j] >> 32;
@@ -213,6 +219,33 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     constexpr size_t kMax = kStepEntriesMax - 4;
     for (size_t c0 = 0; c0 < order.size(); c0 += kMax) {
       const size_t c1 = std::min(order.size(), c0 + kMax);
+      // A ghost step's values: its in-ends' and out-ends' currents, each run
+      // in wire order; an entry's index is its place in its end's run.
+      uint32_t desc = chunk, g0 = 0;
+      if (ghost) {
+        gin.clear();
+        gout.clear();
+        for (size_t q = c0; q < c1; q++) {
+          const uint32_t u = ent[lo + (uint32_t)v[order[q]]];
+          ((u & 2u) ? gout : gin).push_back(u >> 2);
+        }
+        std::sort(gin.begin(), gin.end());
+        std::sort(gout.begin(), gout.end());
+        gidx.resize(c1 - c0);
+        for (size_t q = c0; q < c1; q++) {
+          const uint32_t u = ent[lo + (uint32_t)v[order[q]]];
+          const auto &run = (u & 2u) ? gout : gin;
+          gidx[q - c0] =
+              (uint32_t)(std::lower_bound(run.begin(), run.end(), u >> 2) - run.begin());
+        }
+        g0 = (uint32_t)tp.gsrc.size();
+        for (uint32_t e = 0; e < 2; e++) {
+          const auto &run = e ? gout : gin;
+          for (uint32_t w : run) tp.gsrc.push_back((w << 1) | e);
+          while (tp.gsrc.size() % 4) tp.gsrc.push_back(kTePad);
+        }
+        desc = kGhostStep | ((uint32_t)gin.size() << kGhostCountBits) | (uint32_t)gout.size();
+      }
       // The step's runs (pieces of `order` with one node), by owning warp.
       for (auto &wr : wruns) wr.clear();
       for (size_t q = c0; q < c1;) {
@@ -221,7 +254,7 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
         wruns[node_of(order[q]) % kTileWarps].emplace_back((uint32_t)(e - q), (uint32_t)q);
         q = e;
       }
-      const uint32_t b0 = (uint32_t)tp.ent.size(), g0 = (uint32_t)tp.gw.size();
+      const uint32_t b0 = (uint32_t)tp.ent.size();
       for (uint32_t h = 0; h < kStepHeaderWords; h++) tp.ent.push_back(0u);
       std::vector<uint16_t> hdr(2 * kStepHeaderWords, 0);
       uint32_t n = 0;
@@ -242,21 +275,19 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
           hdr[32 * w + L] = (uint16_t)n;
           for (uint32_t r : lane_runs[L])
             for (uint32_t k = 0; k < wr[r].first; k++) {
-              const uint32_t j = order[wr[r].second + k];
-              tp.ent.push_back(word(v[j], k == 0));
-              if (gather) tp.gw.push_back(ent[lo + (uint32_t)v[j]] >> 2);
+              const size_t q = wr[r].second + k;
+              uint32_t wd = word(v[order[q]], k == 0);
+              if (ghost) wd = (wd & ~(kChunkWires - 1)) | gidx[q - c0];
+              tp.ent.push_back(wd);
               n++;
             }
         }
       }
-      hdr[kTileLanes] = (uint16_t)(n | (gather ? kStepGatherFlag : 0u));
+      hdr[kTileLanes] = (uint16_t)n;
       for (uint32_t h = 0; h < kStepHeaderWords; h++)
         tp.ent[b0 + h] = (uint32_t)hdr[2 * h] | ((uint32_t)hdr[2 * h + 1] << 16);
-      while ((tp.ent.size() - b0) % 4) {  // 16-byte blocks for the bulk copies
-        tp.ent.push_back(kTePad);
-        if (gather) tp.gw.push_back(0u);
-      }
-      tp.steps.push_back(make_uint4(b0, (uint32_t)tp.ent.size() - b0, chunk, g0));
+      while ((tp.ent.size() - b0) % 4) tp.ent.push_back(kTePad);  // 16-byte blocks for the bulk copies
+      tp.steps.push_back(make_uint4(b0, (uint32_t)tp.ent.size() - b0, desc, g0));
     }
   };
   auto flush_sparse = [&]() {
@@ -264,7 +295,7 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     // One wire range: order by (node, CSR position) only.
     for (uint64_t &k : sparse) k &= (1ull << 45) - 1;
     std::sort(sparse.begin(), sparse.end());
-    emit(sparse, 0, sparse.size(), kGatherStep);
+    emit(sparse, 0, sparse.size(), true, 0u);
     sparse.clear();
   };
   sparse.clear();
@@ -274,7 +305,7 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
     while (b < keys.size() && (keys[b] >> 45) == chunk) b++;
     if (b - a >= kDenseMin) {
       flush_sparse();
-      emit(keys, a, b, (uint32_t)chunk);
+      emit(keys, a, b, false, (uint32_t)chunk);
     } else {
       sparse.insert(sparse.end(), keys.begin() + a, keys.begin() + b);
     }
@@ -304,19 +335,43 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
                   plans[t], keys, sparse);
     });
   for (auto &th : pool) th.join();
-  std::vector<uint32_t> tile_step(T + 1, 0), all_ent, all_gw;
+  std::vector<uint32_t> tile_step(T + 1, 0), all_ent;
   std::vector<uint4> steps;
+  std::vector<uint2> glist;  // {slot, wire << 1 | end}
+  int64_t gslots = 0;
   for (uint32_t t = 0; t < T; t++) {
     tile_step[t] = (uint32_t)steps.size();
-    const uint32_t eb = (uint32_t)all_ent.size(), gb = (uint32_t)all_gw.size();
+    const uint32_t eb = (uint32_t)all_ent.size(), gb = (uint32_t)gslots;
     for (uint4 s : plans[t].steps) steps.push_back(make_uint4(s.x + eb, s.y, s.z, s.w + gb));
     all_ent.insert(all_ent.end(), plans[t].ent.begin(), plans[t].ent.end());
-    all_gw.insert(all_gw.end(), plans[t].gw.begin(), plans[t].gw.end());
+    for (size_t k = 0; k < plans[t].gsrc.size(); k++)
+      if (plans[t].gsrc[k] != kTePad) glist.push_back(make_uint2(gb + (uint32_t)k, plans[t].gsrc[k]));
+    gslots += (int64_t)plans[t].gsrc.size();
+    if (all_ent.size() > 0xffffffffull || gslots > 0x7fffffffll)
+      return set_error(CKT_EINVAL, "tiled plan too large for 32-bit offsets");
     std::vector<uint4>().swap(plans[t].steps);
     std::vector<uint32_t>().swap(plans[t].ent);
-    std::vector<uint32_t>().swap(plans[t].gw);
+    std::vector<uint32_t>().swap(plans[t].gsrc);
   }
   tile_step[T] = (uint32_t)steps.size();
+  // Packing order: by source block of kPackWires wires, then by slot, so
+  // that a block's stores into one step's run are consecutive.
+  std::sort(glist.begin(), glist.end(), [](const uint2 &x, const uint2 &y) {
+    const uint32_t bx = (x.y >> 1) / kPackWires, by = (y.y >> 1) / kPackWires;
+    return bx != by ? bx < by : x.x < y.x;
+  });
+  const uint32_t nblocks = (uint32_t)((g->W + kPackWires - 1) / kPackWires);
+  if (glist.size() > kPackFirstMask)
+    return set_error(CKT_EINVAL, "too many ghost contributions for the packing list");
+  std::vector<uint32_t> gblock(nblocks + 1, 0u);
+  for (size_t k = glist.size(); k-- > 0;) {
+    const uint32_t b = (glist[k].y >> 1) / kPackWires;
+    gblock[b] = (gblock[b] & ~kPackFirstMask) | (uint32_t)k |
+                ((glist[k].y & 1u) ? kPackHasOut : kPackHasIn);
+  }
+  gblock[nblocks] = (uint32_t)glist.size();
+  for (uint32_t b = nblocks; b-- > 0;)  // blocks without entries start where the next one does
+    if ((gblock[b] & (kPackHasIn | kPackHasOut)) == 0u) gblock[b] = gblock[b + 1] & kPackFirstMask;
   // Per tile, the nodes whose folds are added when the tile finishes: not
   // private and touched by at least one wire.
   std::vector<uint32_t> mask((size_t)T * (kTileNodesMax / 32), 0u);
@@ -325,13 +380,25 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
       const uint32_t t = x / tile_nodes, i = x % tile_nodes;
       mask[(size_t)t * (kTileNodesMax / 32) + i / 32] |= 1u << (i % 32);
     }
+  // Staged packing once the ghost ends average kPackWires / 8 per source
+  // block: below that, reading whole slices costs more than the scattered
+  // stores it saves.
+  g->ghost_staged = (int64_t)glist.size() * 8 >= (int64_t)nblocks * kPackWires;
   int rc;
   if ((rc = upload(&g->tile_step, tile_step, &g->device_bytes)) ||
       (rc = upload(&g->tile_steps, steps, &g->device_bytes)) ||
       (rc = upload(&g->tile_ent, all_ent, &g->device_bytes)) ||
-      (rc = upload(&g->tile_gw, all_gw, &g->device_bytes)) ||
-      (rc = upload(&g->tile_mask, mask, &g->device_bytes)))
+      (rc = upload(&g->tile_mask, mask, &g->device_bytes)) ||
+      (rc = upload(&g->ghost_list, glist, &g->device_bytes)) ||
+      (rc = upload(&g->ghost_block, gblock, &g->device_bytes)))
     return rc;
+  g->ghost_blocks = nblocks;
+  CKT_CUDA(cudaMalloc(reinterpret_cast<void **>(&g->ghost),
+                      (size_t)std::max<int64_t>(gslots, 4) * sizeof(float)));
+  g->device_bytes += std::max<int64_t>(gslots, 4) * (int64_t)sizeof(float);
+  g->ghost_slots = gslots;
+  g->ghost_n = (int64_t)glist.size();
+  CKT_CUDA(cudaEventCreateWithFlags(&g->ghost_done, cudaEventDisableTiming));
   void *word = nullptr;
   CKT_CUDA(cudaHostAlloc(&word, sizeof(uint32_t), cudaHostAllocMapped));
   g->tile_error_host = static_cast<volatile uint32_t *>(word);
@@ -341,7 +408,7 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
   g->num_tiles = T;
   g->tile_num_steps = (int64_t)steps.size();
   g->tile_stream_steps = 0;
-  for (const uint4 &s : steps) g->tile_stream_steps += s.z != kGatherStep;
+  for (const uint4 &s : steps) g->tile_stream_steps += (s.z & kGhostStep) == 0u;
   return CKT_OK;
 }
 

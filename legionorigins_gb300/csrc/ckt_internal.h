@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -62,8 +63,13 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 // tile's contributions are cut into steps, each covering an ascending range
 // of wires: a stream step holds entries of one chunk, whose I[0]/I[9] slices
 // the block copies into shared memory whole (a chunk with more entries than
-// a step holds takes consecutive steps); a gather step merges chunks with
-// few of the tile's contributions, whose currents are gathered one by one.
+// a step holds takes consecutive steps); a ghost step merges chunks with few
+// of the tile's contributions, whose currents a packing kernel
+// (ghost_pack_kernel) has first copied, in wire order, into the step's
+// region of the graph's ghost buffer: the in-ends' I[0] values, padded to a
+// multiple of 4, then the out-ends' I[9] values, padded likewise.  The block
+// copies the two runs to the same places a stream step's slices go, so an
+// entry's value sits at end * kChunkWires + index in either kind of step.
 // Steps run in wire order and, inside a step, a node's contributions in
 // wire order, so every node still adds its contributions in the CSR's order.
 // Inside a step, entries are grouped by the consumer warp that owns their
@@ -71,27 +77,34 @@ constexpr int64_t kMaxWires = (int64_t)1 << 29;  // 2W entries and offsets fit 3
 // lanes as whole runs, longest first to the least-loaded lane.  A step's
 // block is a header of kStepHeaderWords words -- 16-bit offsets: lane list
 // l = 32 w + L starts at header[l] (l < kTileLanes), header[kTileLanes] =
-// entries | (gather ? kStepGatherFlag : 0) -- followed by the entries,
-// padded to a multiple of 4.
-//   step record: {first block word, block words, chunk or kGatherStep,
-//                 first gather-wire slot (parallel to the entries)}
-//   entry word: wire within chunk (kChunkBits) | end | node within tile
+// entries -- followed by the entries, padded to a multiple of 4.
+//   step record: {first block word, block words, chunk or ghost descriptor,
+//                 first ghost slot}
+//   ghost descriptor: kGhostStep | in-end count << kGhostCountBits | out-end count
+//   entry word: index (kChunkBits: wire within chunk, or position within
+//               the step's in- or out-end run) | end | node within tile
 //               (13 bits) | flush | head | private, from the low bit up
 // flush: the entry starts a new piece group and is not the node's first;
 // head: first entry of its node within the step.  Padding words are kTePad.
+//   ghost list entry (ghost_pack_kernel): {slot, wire << 1 | end}, sorted by
+//   (wire / kPackWires, slot); ghost_block[b] = first entry of source block
+//   b (wires [b kPackWires, (b + 1) kPackWires)) | kPackHasIn | kPackHasOut.
 constexpr uint32_t kTileNodesMax = 8192;
 constexpr uint32_t kChunkBits = 12;
 constexpr uint32_t kChunkWires = 1u << kChunkBits;
-constexpr uint32_t kGatherStep = 0xffffffffu;
+constexpr uint32_t kGhostStep = 0x80000000u, kGhostCountBits = 13,
+                   kGhostCountMask = (1u << kGhostCountBits) - 1u;
+constexpr uint32_t kPackWires = 4096, kPackHasIn = 1u << 30, kPackHasOut = 1u << 31,
+                   kPackFirstMask = kPackHasIn - 1u;
 constexpr uint32_t kTeEnd = 1u << kChunkBits, kTeNodeShift = kChunkBits + 1,
                    kTeFlush = 1u << (kTeNodeShift + 13), kTeHead = kTeFlush << 1,
                    kTePriv = kTeHead << 1, kTePad = 0xffffffffu;
 constexpr uint32_t kStepEntriesMax = kChunkWires;  // padded entries of one step
 static_assert(kTePriv < (1u << 31), "entry word fields overflow");
+static_assert(kStepEntriesMax <= kGhostCountMask, "ghost counts overflow");
 constexpr uint32_t kTileWarps = 31;                // consumer warps of a block
 constexpr uint32_t kTileLanes = 32 * kTileWarps;   // consumer lanes
 constexpr uint32_t kStepHeaderWords = ((kTileLanes + 1 + 1) / 2 + 3) / 4 * 4;
-constexpr uint32_t kStepGatherFlag = 0x8000u;
 
 inline unsigned grid_for(uint64_t n, unsigned block = 256) {
   return (unsigned)((n + block - 1) / block);
@@ -143,7 +156,24 @@ struct ckt_graph {
   uint32_t *tile_step = nullptr;   // [num_tiles + 1]
   uint4 *tile_steps = nullptr;     // [steps]
   uint32_t *tile_ent = nullptr;    // entry words, every step's run 16-byte aligned
-  uint32_t *tile_gw = nullptr;     // gather steps' wire indices, parallel to their entries
+  // Ghost steps' currents: ghost_slots floats, filled before each pass by
+  // ghost_pack_kernel from the ghost_n entries of ghost_list.
+  // ghost_staged: the packing stages whole current slices (many ghost ends
+  // per source block) rather than reading each current directly.
+  float *ghost = nullptr;
+  uint2 *ghost_list = nullptr;
+  uint32_t *ghost_block = nullptr;  // [ghost_blocks + 1]
+  int64_t ghost_slots = 0, ghost_n = 0;
+  uint32_t ghost_blocks = 0;
+  bool ghost_staged = false;
+  // Passes on one graph share its ghost buffer: a pass launched on another
+  // stream than the previous one first waits for the previous one's end
+  // (ghost_done, recorded after every pass), in the order the calls are
+  // made.
+  mutable std::mutex ghost_mu;
+  mutable cudaEvent_t ghost_done = nullptr;
+  mutable cudaStream_t ghost_stream = nullptr;
+  mutable bool ghost_used = false;
   uint32_t *tile_mask = nullptr;   // [num_tiles * kTileNodesMax / 32] bit: the node's
                                    // folds are added at the end (shared/ghost, touched)
   // [1] bit 0: a copy wait timed out.  Pinned host memory mapped for the

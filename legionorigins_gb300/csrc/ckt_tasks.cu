@@ -129,7 +129,7 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   a.tile_step = g->tile_step;
   a.steps = g->tile_steps;
   a.ent = g->tile_ent;
-  a.gw = g->tile_gw;
+  a.ghost = g->ghost;
   a.mask = g->tile_mask;
   a.I0 = w.current;
   a.I9 = w.current + 9 * w.seg_stride;
@@ -145,8 +145,50 @@ static int launch_dc_tile(const ckt_graph *g, const ckt_wires &w, const ckt_node
   a.node_copy = ((reinterpret_cast<uintptr_t>(n.voltage) | reinterpret_cast<uintptr_t>(n.capacitance) |
                   reinterpret_cast<uintptr_t>(n.leakage)) & 15u) == 0;
   a.dt = dt;
-  dc_tile_kernel<UV><<<g->num_tiles, kTileBlock, dc_tile_smem_bytes(g->tile_nodes), s>>>(a);
-  CKT_CHECK_LAUNCH();
+  // The ghost buffer is the graph's: passes on other streams are ordered
+  // behind the previous pass (not inside a stream capture, where the
+  // captured work is ordered by whoever launches the graph).
+  std::lock_guard<std::mutex> lock(g->ghost_mu);
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &capture) != cudaSuccess) {
+    (void)cudaGetLastError();
+    capture = cudaStreamCaptureStatusActive;
+  }
+  const bool order = g->ghost_n > 0 && capture == cudaStreamCaptureStatusNone;
+  if (order && g->ghost_used && g->ghost_stream != s)
+    CKT_CUDA(cudaStreamWaitEvent(s, g->ghost_done, 0));
+  // The tile pass may start while the packing runs (programmatic dependent
+  // launch): its stream steps need only calc_new_currents' results, which
+  // were complete before the packing began; its copy lane waits for the
+  // packing before the first ghost step.
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g->num_tiles);
+  cfg.blockDim = dim3(kTileBlock);
+  cfg.dynamicSmemBytes = dc_tile_smem_bytes(g->tile_nodes);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  if (g->ghost_n > 0) {
+    const uint32_t n = (uint32_t)g->ghost_n;
+    if (g->ghost_staged) {
+      ghost_pack_kernel<true><<<g->ghost_blocks, kPackBlock, 0, s>>>(
+          g->ghost_list, g->ghost_block, n, (uint32_t)g->W, a.I0, a.I9, g->ghost);
+    } else {
+      const uint32_t per_block = kPackBlock * kPackPer;
+      ghost_pack_kernel<false><<<(n + per_block - 1) / per_block, kPackBlock, 0, s>>>(
+          g->ghost_list, g->ghost_block, n, (uint32_t)g->W, a.I0, a.I9, g->ghost);
+    }
+    CKT_CHECK_LAUNCH();
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  CKT_CUDA(cudaLaunchKernelEx(&cfg, dc_tile_kernel<UV>, a));
+  if (order) {
+    CKT_CUDA(cudaEventRecord(g->ghost_done, s));
+    g->ghost_stream = s;
+    g->ghost_used = true;
+  }
   return CKT_OK;
 }
 

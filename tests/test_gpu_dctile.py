@@ -4,9 +4,9 @@ into shared memory chunk by chunk) against the per-node gather form.
 The index-space distribute_charge and the fused node pass take the tiled
 form when the current array is 16-byte aligned and its segment stride is a
 multiple of 4, and the gather form otherwise.  Both must give the same bits
-as each other and as the oracle, on shapes with dense chunks, sparse
-(gathered) chunks, hub nodes whose runs cross many chunks, tiles that
-straddle pieces, and heavy cross-piece reduction.
+as each other and as the oracle, on shapes with dense chunks, sparse chunks
+(packed into the graph's ghost buffer first), hub nodes whose runs cross
+many chunks, tiles that straddle pieces, and heavy cross-piece reduction.
 """
 import ctypes
 
@@ -116,11 +116,11 @@ def test_tiled_equals_gather_and_oracle(cuda, oracle, shape, fused):
     assert steps >= stream >= 0 and err == 0
 
 
-def test_plan_has_stream_and_gather_steps(cuda, oracle):
+def test_plan_has_stream_and_ghost_steps(cuda, oracle):
     """Config-1 pieces (16384 nodes, 65536 wires each): each half-piece tile
     copies every chunk of its own piece (a chunk with more of the tile's
-    entries than a step holds takes two steps) and gathers its ghost
-    contributions."""
+    entries than a step holds takes two steps) and takes its contributions
+    from other pieces' wires through ghost steps."""
     c = oracle.generate(oracle.GenParams(4, 16384, 65536, 95, 12345, L_offset=0.001))
     dc = Strided(cuda, c, 4 * 65536).dc
     tiles, steps, stream, err = tile_info(dc)
@@ -188,6 +188,52 @@ def test_unaligned_node_arrays(cuda, oracle, shape):
         got_b = b.state(cuda)[k]
         assert np.array_equal(got_a[k].view(np.uint32), got_b.view(np.uint32)), (shape, k)
     assert tile_info(b.dc)[3] == 0
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["charge", "fused"])
+def test_one_graph_shared_by_two_streams(cuda, oracle, fused):
+    """Two circuits of one topology, with different states, run on two
+    streams through the same graph, their calls interleaved: the passes
+    share the graph's ghost buffer, so the library orders each pass behind
+    the previous one, and each circuit gets the bits it gets alone."""
+    from legionorigins_gb300 import check, lib
+    from legionorigins_gb300 import circuit as C
+
+    c = oracle.generate(oracle.GenParams(8, 16384, 65536, 50, 21, L_offset=0.001))
+    W = c.params.num_pieces * c.params.wires_per_piece
+    stride = W + (-W) % 4 + 4
+    runs = [Strided(cuda, c, stride) for _ in range(4)]  # a, b shared; a, b alone
+    rng = np.random.default_rng(5)
+    bstate = {k: rng.uniform(-1, 1, getattr(c, k).shape).astype(np.float32)
+              for k in ("current", "voltage")}
+    for r in (runs[1], runs[3]):
+        for k, v in bstate.items():
+            r.dc.t[k][:, :W] = cuda.from_numpy(v).cuda()
+    prm = C.params(1, 0)
+    L, g = lib(), runs[0].dc.graph.handle
+    s1, s2 = cuda.cuda.Stream(), cuda.cuda.Stream()
+    cuda.cuda.synchronize()
+
+    def step(r, graph, stream):
+        w, n = r.wires(), r.dc.nodes()
+        check(L.ckt_calc_new_currents_all(graph, w, n, ctypes.byref(prm), stream))
+        if fused:
+            check(L.ckt_distribute_update_all(graph, w, n, ctypes.byref(prm), stream))
+        else:
+            check(L.ckt_distribute_charge_all(graph, w, n, ctypes.byref(prm), stream))
+
+    for _ in range(3):
+        step(runs[0], g, s1.cuda_stream)
+        step(runs[1], g, s2.cuda_stream)
+    for r in runs[2:]:
+        for _ in range(3):
+            step(r, r.dc.graph.handle, None)
+    cuda.cuda.synchronize()
+    for shared, alone in ((runs[0], runs[2]), (runs[1], runs[3])):
+        a, b = shared.state(cuda), alone.state(cuda)
+        for k in STATE:
+            assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    assert tile_info(runs[0].dc)[3] == 0
 
 
 def test_copy_wait_that_runs_out_reports_and_recovers(cuda, oracle):

@@ -3,8 +3,10 @@
 The plan builder (legionorigins_gb300/csrc/ckt_graph.cpp) is compiled with
 g++ into a small checker that builds random graphs through build_node_csr,
 plans every tile, and replays the GPU kernel's walk over the plan exactly
-(stream steps read the chunk's staged currents, gather steps read through
-the wire indices; every consumer lane sums its list of whole node runs,
+(stream steps read the chunk's staged currents, ghost steps the runs of
+in-end and out-end currents the packing kernel stores for them, checked to
+be each the step's wires in order; every consumer lane sums its list of
+whole node runs,
 private nodes in place, shared/ghost nodes through folds flushed at group
 starts).  The result must equal, bit for bit, the sequential sum in CSR
 order that the gather form computes; the plan's layout invariants (16-byte
@@ -99,23 +101,44 @@ static int run(int P, int npp, int wpp, int nshared, double pct, uint64_t seed) 
     const uint32_t x0 = t * TN, xe = std::min<uint32_t>(N, x0 + TN), nn = xe - x0;
     plan_tile(off.data(), ent.data(), x0, xe, tp, keys, sparse);
     std::vector<float> sacc(q0.begin() + x0, q0.begin() + xe), sfold(nn, 0.f);
-    if (tp.ent.size() % 4 || tp.gw.size() % 4) FAIL("tile arrays not in 16-byte units");
+    if (tp.ent.size() % 4 || tp.gsrc.size() % 4) FAIL("tile arrays not in 16-byte units");
     for (const uint4 &st : tp.steps) {
       if (st.x % 4 || st.y % 4 || st.w % 4) FAIL("step block not 16-byte aligned");
       if (st.y < kStepHeaderWords || st.y > kStepHeaderWords + kStepEntriesMax)
         FAIL("step block size %u", st.y);
-      const bool stream = st.z != kGatherStep;
+      const bool stream = (st.z & kGhostStep) == 0u;
       const uint16_t *hdr = reinterpret_cast<const uint16_t *>(tp.ent.data() + st.x);
-      const uint32_t last = hdr[kTileLanes], total = last & ~kStepGatherFlag;
-      if (((last & kStepGatherFlag) == 0) != stream) FAIL("gather flag");
+      const uint32_t total = hdr[kTileLanes];
       if (total > st.y - kStepHeaderWords) FAIL("entry count");
       const uint32_t *sent = tp.ent.data() + st.x + kStepHeaderWords;
       std::vector<float> sval(2 * kChunkWires, 0.f);
-      if (stream)
+      uint32_t nrun[2] = {kChunkWires, kChunkWires};
+      if (stream) {
         for (uint32_t i = 0; i < kChunkWires && st.z * kChunkWires + i < (uint32_t)W; i++) {
           sval[i] = I0[st.z * kChunkWires + i];
           sval[kChunkWires + i] = I9[st.z * kChunkWires + i];
         }
+      } else {
+        nrun[0] = (st.z >> kGhostCountBits) & kGhostCountMask;
+        nrun[1] = st.z & kGhostCountMask;
+        if (nrun[0] + nrun[1] != total) FAIL("ghost values %u + %u for %u entries", nrun[0], nrun[1], total);
+        uint32_t g = st.w;
+        for (uint32_t e = 0; e < 2; e++) {
+          const uint32_t np = (nrun[e] + 3u) & ~3u;
+          if (g + np > tp.gsrc.size()) FAIL("ghost run out of bounds");
+          for (uint32_t i = 0; i < np; i++) {
+            const uint32_t src = tp.gsrc[g + i];
+            if (i >= nrun[e]) {
+              if (src != kTePad) FAIL("ghost padding");
+              continue;
+            }
+            if (src == kTePad || (src & 1u) != e) FAIL("ghost slot end");
+            if (i > 0 && src <= tp.gsrc[g + i - 1]) FAIL("ghost run not in wire order");
+            sval[e * kChunkWires + i] = e ? I9[src >> 1] : I0[src >> 1];
+          }
+          g += np;
+        }
+      }
       std::vector<int> seen(nn, 0);
       for (uint32_t l = 0; l < kTileLanes; l++) {
         const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : total;
@@ -124,8 +147,8 @@ static int run(int P, int npp, int wpp, int nshared, double pct, uint64_t seed) 
         float acc = 0.f, fold = 0.f;
         for (uint32_t p = b; p < e; p++) {
           const uint32_t u = sent[p], end = (u & kTeEnd) ? 1u : 0u;
-          const float v = stream ? sval[end * kChunkWires + (u & (kChunkWires - 1))]
-                                 : (end ? I9[tp.gw[st.w + p]] : I0[tp.gw[st.w + p]]);
+          if ((u & (kChunkWires - 1)) >= nrun[end]) FAIL("ghost index out of its run");
+          const float v = sval[end * kChunkWires + (u & (kChunkWires - 1))];
           const uint32_t x = (u >> kTeNodeShift) & (kTileNodesMax - 1);
           if (u & kTeHead) {
             if (node != 0xffffffffu) { sacc[node] = acc; sfold[node] = fold; }
@@ -163,7 +186,7 @@ static int run(int P, int npp, int wpp, int nshared, double pct, uint64_t seed) 
 
 int main() {
   struct { int P, npp, wpp, ns; double pct; } cases[] = {
-      {16, 2048, 8192, 256, 95},    // dense chunks, ghost contributions gathered
+      {16, 2048, 8192, 256, 95},    // dense chunks, ghost contributions packed
       {4, 8192, 16384, 4096, 50},   // heavy cross-piece reduction
       {8, 1000, 4003, 100, 80},     // ragged wire count, tiles spanning pieces
       {3, 5, 7, 2, 50},             // tiny
