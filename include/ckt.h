@@ -256,6 +256,15 @@ int ckt_sanity_check_pieces_noalloc(const ckt_piece *pieces, int32_t num_pieces,
  * ---------------------------------------------------------------------- */
 int ckt_calc_new_currents_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                               const ckt_params *prm, void *stream);
+/* ckt_distribute_charge_all and ckt_distribute_update_all launch two
+ * kernels: one packs the currents of the graph's sparse contributions (in
+ * the benchmark circuits, wires ending in another piece) into a buffer the
+ * graph owns, and the tiled pass reads them from there.  Calls on one graph
+ * may come from several streams and host threads: each pass made on another
+ * stream than the previous pass on the graph first waits for that pass, in
+ * the order the calls are made.  Inside a stream capture the calls add no
+ * such wait, and the captured graph must not overlap other passes on the same
+ * ckt_graph. */
 int ckt_distribute_charge_all(const ckt_graph *graph, ckt_wires wires, ckt_nodes nodes,
                               const ckt_params *prm, void *stream);
 int ckt_update_voltages_all(const ckt_graph *graph, ckt_nodes nodes, void *stream);
