@@ -219,6 +219,7 @@ TOOLS_SIGNATURES = {
     "ckt_check_dt_quotient": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _P, _P]),
     "ckt_check_recip_quotient": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _I32, _I32, _P,
                                                 _P]),
+    "ckt_check_wide_quotient": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _I32, _P, _P]),
 }
 
 _lib = None

@@ -170,10 +170,11 @@ struct DualFast {
 //   voltages:  a3_k = dt (i_k - i_k+1), v_k+1 <- V0_k + a3_k / C
 // Each phase first forms all of its dividends, then takes the corrected
 // quotients when every dividend of the thread's two wires lies in the
-// guarded range, and the divide routine otherwise (zero dividends, as in a
-// loop's first step, large ones while the recurrence overflows, tiny ones).
-// Both branches round every quotient to the same float, so the bits never
-// depend on which one ran.  DTF: dt is (float)1e-6 and its quotients use the
+// guarded range, and wide_quot otherwise (zero dividends, as in a loop's
+// first step, large ones and infinities while the recurrence overflows),
+// the divide routine only for dividends too tiny for wide_quot.  Every
+// branch rounds every quotient to the same float, so the bits never depend
+// on which one ran.  DTF: dt is (float)1e-6 and its quotients use the
 // split reciprocal (2 operations); otherwise they are corrected quotients too.
 template <bool DTF>
 struct DualExact {
@@ -222,41 +223,70 @@ struct DualExact {
       bad |= dt_outside(a1[k].x) | dt_outside(a1[k].y) | outside(a2[k].x, kRLo, kRHi) |
              outside(a2[k].y, kRLo, kRHi);
     }
+    // A phase that leaves the corrected quotient (zeros, huge values and
+    // infinities as a loop's state starts or blows up) takes wide_quot, and
+    // the divide routine only for the rare dividends wide_quot does not
+    // cover: with DTF a dt dividend below kDtTiny (whose split quotient may
+    // be off) or an R dividend below kRTiny, a C dividend below kCTiny;
+    // without DTF, phase 1 always.
+    bool wide = false;  // phase 1 left the corrected quotient
     if (!bad) {
 #pragma unroll
       for (int k = 0; k < 10; k++) ni[k] = recip_quot2(a2[k], kR);
     } else {
-      const float2 R = make_float2(-kR.nb.x, -kR.nb.y);
+      bool rare = !DTF;
+      if (DTF) {
 #pragma unroll
-      for (int k = 0; k < 10; k++) {
-        const float dx = __fsub_rn(nv[k + 1].x, nv[k].x), dy = __fsub_rn(nv[k + 1].y, nv[k].y);
-        ni[k] = make_float2(__fdiv_rn(__fsub_rn(dx, __fdiv_rn(a1[k].x, dt)), R.x),
-                            __fdiv_rn(__fsub_rn(dy, __fdiv_rn(a1[k].y, dt)), R.y));
+        for (int k = 0; k < 10; k++)
+          rare |= tiny_nonzero(a1[k].x, kDtTiny) | tiny_nonzero(a1[k].y, kDtTiny) |
+                  tiny_nonzero(a2[k].x, kRTiny) | tiny_nonzero(a2[k].y, kRTiny);
       }
+      if (!rare) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) ni[k] = wide_quot2(a2[k], kR, kRLo, kRHi);
+      } else {
+        const float2 R = make_float2(-kR.nb.x, -kR.nb.y);
+#pragma unroll
+        for (int k = 0; k < 10; k++) {
+          const float dx = __fsub_rn(nv[k + 1].x, nv[k].x), dy = __fsub_rn(nv[k + 1].y, nv[k].y);
+          ni[k] = make_float2(__fdiv_rn(__fsub_rn(dx, __fdiv_rn(a1[k].x, dt)), R.x),
+                              __fdiv_rn(__fsub_rn(dy, __fdiv_rn(a1[k].y, dt)), R.y));
+        }
+      }
+      wide = true;
     }
     // With DTF, currents from corrected quotients are at most 2^100 / 2^-8
     // in magnitude, so |a3| <= dt 2^109 < 2^90: only the lower bound needs a
-    // check.  Currents from the divide routine may be anything, so a phase 1
-    // that took it sends phase 2 there too.
+    // check.  Currents from a phase 1 that left them may be anything.
     float2 a3[9];
-    bad = DTF ? bad : false;
+    bad = false;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       a3[k] = __fmul2_rn(dt2, __ffma2_rn(ni[k + 1], neg1, ni[k]));
-      if (DTF)
-        bad |= (fabsf(a3[k].x) < kCLo) | (fabsf(a3[k].y) < kCLo);
-      else
-        bad |= outside(a3[k].x, kCLo, kCHi) | outside(a3[k].y, kCLo, kCHi);
+      bad |= (fabsf(a3[k].x) < kCLo) | (fabsf(a3[k].y) < kCLo);
+    }
+    if (!DTF || wide) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) bad |= (fabsf(a3[k].x) > kCHi) | (fabsf(a3[k].y) > kCHi);
     }
     if (!bad) {
 #pragma unroll
       for (int k = 0; k < 9; k++) nv[k + 1] = __fadd2_rn(V0[k], recip_quot2(a3[k], kC));
     } else {
-      const float2 C = make_float2(-kC.nb.x, -kC.nb.y);
+      bool rare = false;
 #pragma unroll
       for (int k = 0; k < 9; k++)
-        nv[k + 1] = make_float2(__fadd_rn(V0[k].x, __fdiv_rn(a3[k].x, C.x)),
-                                __fadd_rn(V0[k].y, __fdiv_rn(a3[k].y, C.y)));
+        rare |= tiny_nonzero(a3[k].x, kCTiny) | tiny_nonzero(a3[k].y, kCTiny);
+      if (!rare) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) nv[k + 1] = __fadd2_rn(V0[k], wide_quot2(a3[k], kC, kCLo, kCHi));
+      } else {
+        const float2 C = make_float2(-kC.nb.x, -kC.nb.y);
+#pragma unroll
+        for (int k = 0; k < 9; k++)
+          nv[k + 1] = make_float2(__fadd_rn(V0[k].x, __fdiv_rn(a3[k].x, C.x)),
+                                  __fadd_rn(V0[k].y, __fdiv_rn(a3[k].y, C.y)));
+      }
     }
   }
   // step() for a state whose 10 currents and 9 wire voltages are all NaN,
@@ -348,32 +378,55 @@ struct SoloExact {
       if (!DTF) bad |= outside(a1[k], kCLo, kCHi);
       bad |= outside(a2[k], kRLo, kRHi);
     }
+    // Leaving the corrected quotient as DualExact::step does.
+    bool wide = false;
     if (!bad) {
 #pragma unroll
       for (int k = 0; k < 10; k++) ni[k] = recip_quot(a2[k], kR);
     } else {
-      const float R = -kR.nb;
+      bool rare = !DTF;
+      if (DTF) {
 #pragma unroll
-      for (int k = 0; k < 10; k++)
-        ni[k] = __fdiv_rn(__fsub_rn(__fsub_rn(nv[k + 1], nv[k]), __fdiv_rn(a1[k], dt)), R);
+        for (int k = 0; k < 10; k++)
+          rare |= tiny_nonzero(a1[k], kDtTiny) | tiny_nonzero(a2[k], kRTiny);
+      }
+      if (!rare) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) ni[k] = wide_quot(a2[k], kR, kRLo, kRHi);
+      } else {
+        const float R = -kR.nb;
+#pragma unroll
+        for (int k = 0; k < 10; k++)
+          ni[k] = __fdiv_rn(__fsub_rn(__fsub_rn(nv[k + 1], nv[k]), __fdiv_rn(a1[k], dt)), R);
+      }
+      wide = true;
     }
     float a3[9];
-    bad = DTF ? bad : false;
+    bad = false;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
       a3[k] = __fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1]));
-      if (DTF)
-        bad |= fabsf(a3[k]) < kCLo;
-      else
-        bad |= outside(a3[k], kCLo, kCHi);
+      bad |= fabsf(a3[k]) < kCLo;
+    }
+    if (!DTF || wide) {
+#pragma unroll
+      for (int k = 0; k < 9; k++) bad |= fabsf(a3[k]) > kCHi;
     }
     if (!bad) {
 #pragma unroll
       for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], recip_quot(a3[k], kC));
     } else {
-      const float C = -kC.nb;
+      bool rare = false;
 #pragma unroll
-      for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(a3[k], C));
+      for (int k = 0; k < 9; k++) rare |= tiny_nonzero(a3[k], kCTiny);
+      if (!rare) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], wide_quot(a3[k], kC, kCLo, kCHi));
+      } else {
+        const float C = -kC.nb;
+#pragma unroll
+        for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(a3[k], C));
+      }
     }
   }
 };

@@ -120,6 +120,77 @@ __global__ void __launch_bounds__(256)
   warp_add(counts + 2, drawn);
 }
 
+// wide_quot, the quotient of EXACT mode's phases that leave the guarded
+// range, against the divide routine: dividends of every class -- huge up to
+// FLT_MAX, tiny down to the divisor's bound, the guarded range, zeros,
+// infinities, NaN, quotients within an ulp of a rounding boundary or of the
+// overflow threshold -- except the nonzero ones below the bound, which the
+// steppers leave to the divide routine.
+__global__ void __launch_bounds__(256)
+    wide_quotient_check_kernel(uint64_t seed, uint64_t count, int32_t divisor,
+                               unsigned long long *counts) {
+  const int be0 = divisor == 0 ? -8 : -30, be1 = -be0 - 1;
+  const float lo = divisor == 0 ? kRLo : kCLo, hi = divisor == 0 ? kRHi : kCHi;
+  const float tiny = divisor == 0 ? kRTiny : kCTiny;
+  const int tiny_e = divisor == 0 ? -118 : -96, lo_e = divisor == 0 ? -50 : -40,
+            hi_e = divisor == 0 ? 100 : 90;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t rounds = (count + stride - 1) / stride;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t bad = 0, out = 0, drawn = 0;
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t i = r * stride + t;
+    if (i >= count) continue;
+    const uint64_t h1 = mix64(seed * 0x9e3779b97f4a7c15ull + 2 * i + 1);
+    const uint64_t h2 = mix64(h1 ^ 0x632be59bd9b4e019ull);
+    const float b = rand_float(h1, be0, be1);
+    const float sgn = (h2 >> 20) & 1u ? -1.0f : 1.0f;
+    const float fmax = __uint_as_float(0x7f7fffffu);
+    float a;
+    switch ((uint32_t)((h2 >> 56) % 8u)) {
+      case 0:
+        a = rand_float(h2, hi_e, 127);
+        break;
+      case 1:
+        a = rand_float(h2, tiny_e, lo_e - 1);
+        break;
+      case 2: {
+        const float sp[8] = {0.0f, __uint_as_float(0x7f800000u), __uint_as_float(0x7fc00000u),
+                             fmax, lo, hi, __uint_as_float(__float_as_uint(hi) + 1u),
+                             __uint_as_float(__float_as_uint(lo) - 1u)};
+        a = sgn * sp[(h2 >> 8) & 7u];
+        break;
+      }
+      case 3: {
+        const double m = (double)fmax + 0x1p103 * ((double)((h2 >> 8) & 7u) - 3.5) / 2.0;
+        a = sgn * __double2float_rn((double)b * m);
+        a = __uint_as_float(__float_as_uint(a) + (uint32_t)((h2 >> 12) & 3u) - 1u);
+        break;
+      }
+      case 4:
+      case 5: {
+        const float q = (h2 >> 9) & 1u ? rand_float(h2, 60, 126) : rand_float(h2, -125, -60);
+        const double mid = (double)q + 0.5 * ((double)__uint_as_float(__float_as_uint(fabsf(q)) + 1u) -
+                                              (double)fabsf(q)) * (q < 0.0f ? -1.0 : 1.0);
+        a = __double2float_rn((double)b * mid);
+        a = __uint_as_float(__float_as_uint(a) + (uint32_t)((h2 >> 12) & 7u) - 3u);
+        break;
+      }
+      default:
+        a = rand_float(h2, -126, 127);
+        break;
+    }
+    if (tiny_nonzero(a, tiny)) continue;
+    const Recip k = make_recip(b);
+    bad += !same_float(wide_quot(a, k, lo, hi), __fdiv_rn(a, b));
+    out += outside(a, lo, hi);
+    drawn++;
+  }
+  warp_add(counts + 0, bad);
+  warp_add(counts + 1, out);
+  warp_add(counts + 2, drawn);
+}
+
 }  // namespace ckt
 
 using namespace ckt;
@@ -155,6 +226,21 @@ extern "C" int ckt_check_recip_quotient(uint64_t seed, uint64_t count, int32_t d
   const unsigned grid = (unsigned)std::min<uint64_t>(want, (uint64_t)sms * 8);
   recip_quotient_check_kernel<<<grid, 256, 0, as_stream(stream)>>>(seed, count, divisor,
                                                                    near_ties, counts);
+  CKT_CHECK_LAUNCH();
+  return CKT_OK;
+}
+
+extern "C" int ckt_check_wide_quotient(uint64_t seed, uint64_t count, int32_t divisor,
+                                       unsigned long long *counts, void *stream) {
+  CKT_REQUIRE(counts != nullptr, "counts is NULL");
+  CKT_REQUIRE(divisor == 0 || divisor == 1, "divisor must be 0 (R) or 1 (C), got %d", divisor);
+  if (count == 0) return CKT_OK;
+  int dev = 0, sms = 0;
+  CKT_CUDA(cudaGetDevice(&dev));
+  CKT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint64_t want = (count + 255) / 256;
+  const unsigned grid = (unsigned)std::min<uint64_t>(want, (uint64_t)sms * 8);
+  wide_quotient_check_kernel<<<grid, 256, 0, as_stream(stream)>>>(seed, count, divisor, counts);
   CKT_CHECK_LAUNCH();
   return CKT_OK;
 }

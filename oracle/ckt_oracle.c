@@ -14,6 +14,7 @@
 #define _XOPEN_SOURCE 700
 #include "ckt_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -719,4 +720,124 @@ void ocl_split_quotient_check(uint64_t lo, uint64_t hi, float dt, float zh, floa
   }
   *bad_trusted = bt;
   *bad_other = bo;
+}
+
+/* The R and C quotients of calc_new_currents (apps/circuit/circuit.cc:
+ * 394-400, circuit_gpu.cu:123-128) as the GPU's EXACT mode evaluates a
+ * dividend outside the corrected quotient's guarded range [lo, hi]: scaled
+ * by 2^-64 (above hi) or 2^80 (below lo) into it, divided by the corrected
+ * quotient (q0 = fmaf(a, y, a*yl), r = fmaf(q0, -b, a), q = fmaf(r, y, q0)
+ * with y = RN(1/b), yl = RN(1/b - y)), and scaled back; zeros and
+ * infinities as a*y.  Draws `n` (dividend, divisor) pairs from seed --
+ * divisors in [2^-8, 2^8) (divisor 0, R) or [2^-30, 2^30) (1, C), dividends
+ * from every class: huge up to FLT_MAX, tiny down to the bound `tiny`, the
+ * guarded range, zeros, infinities, NaN, and values whose quotient lies
+ * within an ulp of a rounding boundary or of the overflow threshold -- and
+ * counts the pairs whose result differs from the IEEE quotient a/b
+ * (`bad`; equal means equal bits, or both NaN), the pairs taken outside
+ * [lo, hi] (`outside`) and all pairs drawn.  Nonzero dividends below
+ * `tiny` are not drawn: the GPU leaves them to its divide routine. */
+static uint64_t wq_mix(uint64_t x)
+{
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+static float wq_bits(uint32_t u)
+{
+  float f;
+  memcpy(&f, &u, sizeof f);
+  return f;
+}
+
+static uint32_t wq_u(float f)
+{
+  uint32_t u;
+  memcpy(&u, &f, sizeof u);
+  return u;
+}
+
+/* A float of random sign and mantissa with binary exponent in [e0, e1]. */
+static float wq_rand(uint64_t h, int e0, int e1)
+{
+  const int e = e0 + (int)((uint32_t)(h >> 32) % (uint32_t)(e1 - e0 + 1));
+  return wq_bits((uint32_t)((e + 127) << 23) | ((uint32_t)h & 0x7fffffu) |
+                 ((uint32_t)(h >> 23) & 0x80000000u));
+}
+
+static float wq_recip_quot(float a, float y, float yl, float nb)
+{
+  const float q0 = fmaf(a, y, a * yl);
+  const float r = fmaf(q0, nb, a);
+  return fmaf(r, y, q0);
+}
+
+static float wq_wide_quot(float a, float y, float yl, float nb, float lo, float hi)
+{
+  const float m = fabsf(a);
+  const float s = m > hi ? 0x1p-64f : (m < lo ? 0x1p80f : 1.0f);
+  const float u = m > hi ? 0x1p64f : (m < lo ? 0x1p-80f : 1.0f);
+  const float q = wq_recip_quot(a * s, y, yl, nb) * u;
+  return (m == 0.0f || isinf(m)) ? a * y : q;
+}
+
+void ocl_wide_quotient_check(uint64_t seed, uint64_t n, int divisor, uint64_t *bad,
+                             uint64_t *outside, uint64_t *drawn)
+{
+  const int be0 = divisor == 0 ? -8 : -30, be1 = -be0 - 1;
+  const float lo = divisor == 0 ? 0x1p-50f : 0x1p-40f, hi = divisor == 0 ? 0x1p100f : 0x1p90f;
+  const int tiny_e = divisor == 0 ? -118 : -96, lo_e = divisor == 0 ? -50 : -40,
+            hi_e = divisor == 0 ? 100 : 90;
+  uint64_t nbad = 0, nout = 0, nd = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    const uint64_t h1 = wq_mix(seed * 0x9e3779b97f4a7c15ull + 2 * i + 1);
+    const uint64_t h2 = wq_mix(h1 ^ 0x632be59bd9b4e019ull);
+    const float b = wq_rand(h1, be0, be1);
+    const float sgn = (h2 >> 20) & 1u ? -1.0f : 1.0f;
+    float a;
+    switch ((h2 >> 56) % 8u) {
+      case 0:  /* huge */
+        a = wq_rand(h2, hi_e, 127);
+        break;
+      case 1:  /* tiny, down to the bound */
+        a = wq_rand(h2, tiny_e, lo_e - 1);
+        break;
+      case 2: {  /* special values and the range edges */
+        const float sp[8] = {0.0f, INFINITY, NAN, FLT_MAX, lo, hi, wq_bits(wq_u(hi) + 1u),
+                             wq_bits(wq_u(lo) - 1u)};
+        a = sgn * sp[(h2 >> 8) & 7u];
+        break;
+      }
+      case 3: {  /* a/b within about an ulp of overflowing */
+        const double m = (double)FLT_MAX + ldexp(1.0, 103) * ((double)((h2 >> 8) & 7u) - 3.5) / 2.0;
+        a = sgn * (float)((double)b * m);
+        a = wq_bits(wq_u(a) + (uint32_t)((h2 >> 12) & 3u) - 1u);
+        break;
+      }
+      case 4:
+      case 5: {  /* a/b within about an ulp of a rounding boundary, huge or tiny */
+        const float q = (h2 >> 9) & 1u ? wq_rand(h2, 60, 126) : wq_rand(h2, -125, -60);
+        const double mid = (double)q + 0.5 * ((double)wq_bits(wq_u(fabsf(q)) + 1u) - (double)fabsf(q)) *
+                                           (q < 0.0f ? -1.0 : 1.0);
+        a = (float)((double)b * mid);
+        a = wq_bits(wq_u(a) + (uint32_t)((h2 >> 12) & 7u) - 3u);
+        break;
+      }
+      default:  /* any exponent */
+        a = wq_rand(h2, -126, 127);
+        break;
+    }
+    if (isfinite(a) && a != 0.0f && fabsf(a) < ldexpf(1.0f, tiny_e)) continue;
+    nd++;
+    const float y = 1.0f / b, yl = fmaf(-b, y, 1.0f) / b;
+    const float got = wq_wide_quot(a, y, yl, -b, lo, hi), want = a / b;
+    nout += !(fabsf(a) >= lo && fabsf(a) <= hi);
+    if (!((isnan(got) && isnan(want)) || wq_u(got) == wq_u(want))) nbad++;
+  }
+  *bad = nbad;
+  *outside = nout;
+  *drawn = nd;
 }

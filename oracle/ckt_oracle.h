@@ -20,7 +20,7 @@
  *                       reduction-instance fold/apply order of
  *                       runtime/lowlevel.h:475-492 (pieces applied ascending)
  *   ocl_uv_f32/_f64     apps/circuit/circuit.cc:445-460, :1290-1307
- *   ocl_split_quotient_check
+ *   ocl_split_quotient_check, ocl_wide_quotient_check
  *                       the division by dt of apps/circuit/circuit.cc:391-393
  *                       as the GPU's EXACT mode forms it (split reciprocal),
  *                       against IEEE division, over ranges of dividends
@@ -159,6 +159,12 @@ double ocl_histogram_threads(uint32_t buckets, uint32_t batch_size, uint32_t num
 
 void ocl_split_quotient_check(uint64_t lo, uint64_t hi, float dt, float zh, float zl, float tiny,
                               uint64_t *bad_trusted, uint64_t *bad_other);
+
+/* EXACT mode's quotient by R or C for dividends outside the corrected
+ * quotient's guarded range, against IEEE division, on random pairs of every
+ * dividend class (see the definition). */
+void ocl_wide_quotient_check(uint64_t seed, uint64_t n, int divisor, uint64_t *bad,
+                             uint64_t *outside, uint64_t *drawn);
 
 #ifdef __cplusplus
 }

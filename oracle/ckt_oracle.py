@@ -120,6 +120,8 @@ def lib():
         f32 = ctypes.c_float
         L.ocl_split_quotient_check.argtypes = [u64, u64, f32, f32, f32, f32, P, P]
         L.ocl_split_quotient_check.restype = None
+        L.ocl_wide_quotient_check.argtypes = [u64, u64, i32, P, P, P]
+        L.ocl_wide_quotient_check.restype = None
         _lib = L
     return _lib
 
@@ -381,3 +383,13 @@ def split_quotient_check(lo: int, hi: int, dt: float, zh: float, zl: float, tiny
     bt, bo = ctypes.c_uint64(), ctypes.c_uint64()
     lib().ocl_split_quotient_check(lo, hi, dt, zh, zl, tiny, ctypes.byref(bt), ctypes.byref(bo))
     return bt.value, bo.value
+
+
+def wide_quotient_check(seed: int, n: int, divisor: int):
+    """(bad, outside, drawn) of EXACT mode's quotient by R (divisor 0) or C
+    (1) outside the guarded range against IEEE division; see
+    ocl_wide_quotient_check."""
+    bad, out, drawn = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    lib().ocl_wide_quotient_check(seed, n, divisor, ctypes.byref(bad), ctypes.byref(out),
+                                  ctypes.byref(drawn))
+    return bad.value, out.value, drawn.value

@@ -45,3 +45,20 @@ def test_corrected_quotient_random_pairs(cuda, ckt, divisor, near_ties):
     assert drawn == n
     assert bad == 0
     assert fast > n // 4  # most pairs exercise the corrected quotient itself
+
+
+@pytest.mark.parametrize("divisor", [0, 1], ids=["R", "C"])
+def test_wide_quotient_random_pairs(cuda, ckt, divisor):
+    """The quotient of the phases that leave the guarded range (the state's
+    zeros at the start of a loop, huge values and infinities as it blows
+    up): every class of dividend, the nonzero ones below the divisor's tiny
+    bound excepted, equals __fdiv_rn."""
+    c = counts(cuda, 3)
+    n = 1 << 30
+    ckt.check(ckt.tools().ckt_check_wide_quotient(4321 + divisor, n, divisor, c.data_ptr(), None))
+    cuda.cuda.synchronize()
+    bad, outside, drawn = c.tolist()
+    print(f"divisor {'RC'[divisor]}: {drawn} pairs, {outside} outside the guarded range, "
+          f"{bad} mismatches")
+    assert bad == 0
+    assert drawn > n // 2 and outside > drawn // 2
