@@ -168,8 +168,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // step's block, runs back to back, each opened by a head entry; an entry's
 // current is svals[end * kChunkWires + index].
 __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const float *svals,
-                                                  uint32_t b, uint32_t e, float *sacc,
-                                                  float *sfold, float dt) {
+                                                  uint32_t b, uint32_t e, float2 *ssum,
+                                                  float dt) {
   uint32_t node = 0xffffffffu;
   float acc = 0.0f, fold = 0.0f;
   for (uint32_t p = b; p < e; p++) {
@@ -177,13 +177,11 @@ __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const fl
     const uint32_t end = (u & kTeEnd) ? 1u : 0u;
     const float v = svals[end * kChunkWires + (u & (kChunkWires - 1))];
     if (u & kTeHead) {
-      if (node != 0xffffffffu) {
-        sacc[node] = acc;
-        sfold[node] = fold;
-      }
+      if (node != 0xffffffffu) ssum[node] = make_float2(acc, fold);
       node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
-      acc = sacc[node];
-      fold = sfold[node];
+      const float2 t = ssum[node];
+      acc = t.x;
+      fold = t.y;
     }
     const float c = end ? __fmul_rn(dt, v) : __fmul_rn(-dt, v);
     if (u & kTePriv) {
@@ -196,10 +194,7 @@ __device__ __forceinline__ void dc_tile_lane_walk(const uint32_t *sent, const fl
       fold = __fadd_rn(fold, c);
     }
   }
-  if (node != 0xffffffffu) {
-    sacc[node] = acc;
-    sfold[node] = fold;
-  }
+  if (node != 0xffffffffu) ssum[node] = make_float2(acc, fold);
 }
 
 // Programmatic dependent launch: the tile pass is launched to start while
@@ -296,9 +291,8 @@ template <bool UV>
 __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   extern __shared__ __align__(128) unsigned char dct_smem[];
   const uint32_t TN = a.tile_nodes;
-  float *sacc = reinterpret_cast<float *>(dct_smem);
-  float *sfold = sacc + TN;
-  uint32_t *smask = reinterpret_cast<uint32_t *>(sfold + TN);
+  float2 *ssum = reinterpret_cast<float2 *>(dct_smem);  // per node: running sum, fold
+  uint32_t *smask = reinterpret_cast<uint32_t *>(ssum + TN);
   unsigned char *stage0 = dct_smem + 2 * TN * 4 + kMaskWords * 4;
   uint64_t *full = reinterpret_cast<uint64_t *>(stage0 + kTileStages * kStageBytes);
   uint64_t *empty = full + kTileStages;
@@ -397,8 +391,7 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
     for (uint32_t r = 0; r < kPer; r++) {
       const uint32_t i = threadIdx.x + r * kTileBlock;
       if (i < nn) {
-        sacc[i] = q[r];
-        sfold[i] = 0.0f;
+        ssum[i] = make_float2(q[r], 0.0f);
       }
     }
   }
@@ -451,7 +444,7 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
       const uint32_t last = hdr[kTileLanes];
       const uint32_t l = threadIdx.x;  // consumer lane list (warp * 32 + lane)
       const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : last;
-      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e, sacc, sfold, a.dt);
+      dc_tile_lane_walk(blk + kStepHeaderWords, vals_of(slot), b, e, ssum, a.dt);
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + slot);
     }
@@ -482,8 +475,9 @@ __global__ void __launch_bounds__(kTileBlock, 1) dc_tile_kernel(DcTileArgs a) {
   for (uint32_t r = 0; r < kPer; r++) {
     const uint32_t i = threadIdx.x + r * kTileBlock, x = x0 + i;
     if (i >= nn) break;
-    float q = sacc[i];
-    if ((smask[i >> 5] >> (i & 31u)) & 1u) q = __fadd_rn(q, sfold[i]);
+    const float2 t = ssum[i];
+    float q = t.x;
+    if ((smask[i >> 5] >> (i & 31u)) & 1u) q = __fadd_rn(q, t.y);
     if (UV) {
       float v, cap, leak;
       if (stage_nodes && i < nn4) {
