@@ -316,13 +316,25 @@ void plan_tile(const uint32_t *off, const uint32_t *ent, uint32_t x0, uint32_t x
 
 }  // namespace
 
-// Builds and uploads the tiled distribute_charge plan; tiles are planned
-// in parallel.
-static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
-                           const std::vector<uint32_t> &ent, uint32_t tile_nodes) {
-  // Tile bases and node counts stay 32-bit in the kernel.
-  if (g->N > 0x7fffffff || g->W == 0) return CKT_OK;
-  const uint32_t N = (uint32_t)g->N;
+// The whole-circuit tiled distribute_charge plan, on the host.
+struct HostTilePlan {
+  uint32_t T = 0;                   // tiles
+  std::vector<uint32_t> tile_step;  // [T + 1]
+  std::vector<uint4> steps;
+  std::vector<uint32_t> ent;
+  std::vector<uint2> glist;         // packing list {slot, wire << 1 | end}
+  std::vector<uint32_t> gblock;     // [nblocks + 1]
+  std::vector<uint32_t> mask;       // [T * kTileNodesMax / 32]
+  int64_t gslots = 0;
+  uint32_t nblocks = 0;
+  bool staged = false;
+};
+
+// Plans every tile (in parallel), concatenates the tiles' steps, entries and
+// ghost runs, and builds the packing list and the per-tile fold masks.
+static int make_tile_plan(uint32_t N, int64_t W, const std::vector<uint32_t> &off,
+                          const std::vector<uint32_t> &ent, uint32_t tile_nodes,
+                          HostTilePlan &hp) {
   const uint32_t T = (N + tile_nodes - 1) / tile_nodes;
   std::vector<TilePlan> plans(T);
   const int nthr = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
@@ -335,69 +347,84 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
                   plans[t], keys, sparse);
     });
   for (auto &th : pool) th.join();
-  std::vector<uint32_t> tile_step(T + 1, 0), all_ent;
-  std::vector<uint4> steps;
-  std::vector<uint2> glist;  // {slot, wire << 1 | end}
-  int64_t gslots = 0;
+  hp.T = T;
+  hp.tile_step.assign(T + 1, 0);
+  hp.steps.clear();
+  hp.ent.clear();
+  hp.glist.clear();
+  hp.gslots = 0;
   for (uint32_t t = 0; t < T; t++) {
-    tile_step[t] = (uint32_t)steps.size();
-    const uint32_t eb = (uint32_t)all_ent.size(), gb = (uint32_t)gslots;
-    for (uint4 s : plans[t].steps) steps.push_back(make_uint4(s.x + eb, s.y, s.z, s.w + gb));
-    all_ent.insert(all_ent.end(), plans[t].ent.begin(), plans[t].ent.end());
+    hp.tile_step[t] = (uint32_t)hp.steps.size();
+    const uint32_t eb = (uint32_t)hp.ent.size(), gb = (uint32_t)hp.gslots;
+    for (uint4 s : plans[t].steps) hp.steps.push_back(make_uint4(s.x + eb, s.y, s.z, s.w + gb));
+    hp.ent.insert(hp.ent.end(), plans[t].ent.begin(), plans[t].ent.end());
     for (size_t k = 0; k < plans[t].gsrc.size(); k++)
-      if (plans[t].gsrc[k] != kTePad) glist.push_back(make_uint2(gb + (uint32_t)k, plans[t].gsrc[k]));
-    gslots += (int64_t)plans[t].gsrc.size();
-    if (all_ent.size() > 0xffffffffull || gslots > 0x7fffffffll)
+      if (plans[t].gsrc[k] != kTePad)
+        hp.glist.push_back(make_uint2(gb + (uint32_t)k, plans[t].gsrc[k]));
+    hp.gslots += (int64_t)plans[t].gsrc.size();
+    if (hp.ent.size() > 0xffffffffull || hp.gslots > 0x7fffffffll)
       return set_error(CKT_EINVAL, "tiled plan too large for 32-bit offsets");
     std::vector<uint4>().swap(plans[t].steps);
     std::vector<uint32_t>().swap(plans[t].ent);
     std::vector<uint32_t>().swap(plans[t].gsrc);
   }
-  tile_step[T] = (uint32_t)steps.size();
+  hp.tile_step[T] = (uint32_t)hp.steps.size();
   // Packing order: by source block of kPackWires wires, then by slot, so
   // that a block's stores into one step's run are consecutive.
-  std::sort(glist.begin(), glist.end(), [](const uint2 &x, const uint2 &y) {
+  std::sort(hp.glist.begin(), hp.glist.end(), [](const uint2 &x, const uint2 &y) {
     const uint32_t bx = (x.y >> 1) / kPackWires, by = (y.y >> 1) / kPackWires;
     return bx != by ? bx < by : x.x < y.x;
   });
-  const uint32_t nblocks = (uint32_t)((g->W + kPackWires - 1) / kPackWires);
-  if (glist.size() > kPackFirstMask)
+  hp.nblocks = (uint32_t)((W + kPackWires - 1) / kPackWires);
+  if (hp.glist.size() > kPackFirstMask)
     return set_error(CKT_EINVAL, "too many ghost contributions for the packing list");
-  std::vector<uint32_t> gblock(nblocks + 1, 0u);
-  for (size_t k = glist.size(); k-- > 0;) {
-    const uint32_t b = (glist[k].y >> 1) / kPackWires;
-    gblock[b] = (gblock[b] & ~kPackFirstMask) | (uint32_t)k |
-                ((glist[k].y & 1u) ? kPackHasOut : kPackHasIn);
+  hp.gblock.assign(hp.nblocks + 1, 0u);
+  for (size_t k = hp.glist.size(); k-- > 0;) {
+    const uint32_t b = (hp.glist[k].y >> 1) / kPackWires;
+    hp.gblock[b] = (hp.gblock[b] & ~kPackFirstMask) | (uint32_t)k |
+                   ((hp.glist[k].y & 1u) ? kPackHasOut : kPackHasIn);
   }
-  gblock[nblocks] = (uint32_t)glist.size();
-  for (uint32_t b = nblocks; b-- > 0;)  // blocks without entries start where the next one does
-    if ((gblock[b] & (kPackHasIn | kPackHasOut)) == 0u) gblock[b] = gblock[b + 1] & kPackFirstMask;
-  // Per tile, the nodes whose folds are added when the tile finishes: not
-  // private and touched by at least one wire.
-  std::vector<uint32_t> mask((size_t)T * (kTileNodesMax / 32), 0u);
-  for (uint32_t x = 0; x < N; x++)
-    if (!(off[x] & kPrivateBit) && (off[x + 1] & kOffsetMask) > (off[x] & kOffsetMask)) {
-      const uint32_t t = x / tile_nodes, i = x % tile_nodes;
-      mask[(size_t)t * (kTileNodesMax / 32) + i / 32] |= 1u << (i % 32);
-    }
+  hp.gblock[hp.nblocks] = (uint32_t)hp.glist.size();
+  for (uint32_t b = hp.nblocks; b-- > 0;)  // blocks without entries start where the next one does
+    if ((hp.gblock[b] & (kPackHasIn | kPackHasOut)) == 0u)
+      hp.gblock[b] = hp.gblock[b + 1] & kPackFirstMask;
   // Staged packing once the ghost ends average kPackWires / 8 per source
   // block: below that, reading whole slices costs more than the scattered
   // stores it saves.
-  g->ghost_staged = (int64_t)glist.size() * 8 >= (int64_t)nblocks * kPackWires;
+  hp.staged = (int64_t)hp.glist.size() * 8 >= (int64_t)hp.nblocks * kPackWires;
+  // Per tile, the nodes whose folds are added when the tile finishes: not
+  // private and touched by at least one wire.
+  hp.mask.assign((size_t)T * (kTileNodesMax / 32), 0u);
+  for (uint32_t x = 0; x < N; x++)
+    if (!(off[x] & kPrivateBit) && (off[x + 1] & kOffsetMask) > (off[x] & kOffsetMask)) {
+      const uint32_t t = x / tile_nodes, i = x % tile_nodes;
+      hp.mask[(size_t)t * (kTileNodesMax / 32) + i / 32] |= 1u << (i % 32);
+    }
+  return CKT_OK;
+}
+
+// Builds and uploads the tiled distribute_charge plan.
+static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
+                           const std::vector<uint32_t> &ent, uint32_t tile_nodes) {
+  // Tile bases and node counts stay 32-bit in the kernel.
+  if (g->N > 0x7fffffff || g->W == 0) return CKT_OK;
+  HostTilePlan hp;
   int rc;
-  if ((rc = upload(&g->tile_step, tile_step, &g->device_bytes)) ||
-      (rc = upload(&g->tile_steps, steps, &g->device_bytes)) ||
-      (rc = upload(&g->tile_ent, all_ent, &g->device_bytes)) ||
-      (rc = upload(&g->tile_mask, mask, &g->device_bytes)) ||
-      (rc = upload(&g->ghost_list, glist, &g->device_bytes)) ||
-      (rc = upload(&g->ghost_block, gblock, &g->device_bytes)))
+  if ((rc = make_tile_plan((uint32_t)g->N, g->W, off, ent, tile_nodes, hp))) return rc;
+  if ((rc = upload(&g->tile_step, hp.tile_step, &g->device_bytes)) ||
+      (rc = upload(&g->tile_steps, hp.steps, &g->device_bytes)) ||
+      (rc = upload(&g->tile_ent, hp.ent, &g->device_bytes)) ||
+      (rc = upload(&g->tile_mask, hp.mask, &g->device_bytes)) ||
+      (rc = upload(&g->ghost_list, hp.glist, &g->device_bytes)) ||
+      (rc = upload(&g->ghost_block, hp.gblock, &g->device_bytes)))
     return rc;
-  g->ghost_blocks = nblocks;
+  g->ghost_blocks = hp.nblocks;
+  g->ghost_staged = hp.staged;
   CKT_CUDA(cudaMalloc(reinterpret_cast<void **>(&g->ghost),
-                      (size_t)std::max<int64_t>(gslots, 4) * sizeof(float)));
-  g->device_bytes += std::max<int64_t>(gslots, 4) * (int64_t)sizeof(float);
-  g->ghost_slots = gslots;
-  g->ghost_n = (int64_t)glist.size();
+                      (size_t)std::max<int64_t>(hp.gslots, 4) * sizeof(float)));
+  g->device_bytes += std::max<int64_t>(hp.gslots, 4) * (int64_t)sizeof(float);
+  g->ghost_slots = hp.gslots;
+  g->ghost_n = (int64_t)hp.glist.size();
   CKT_CUDA(cudaEventCreateWithFlags(&g->ghost_done, cudaEventDisableTiming));
   void *word = nullptr;
   CKT_CUDA(cudaHostAlloc(&word, sizeof(uint32_t), cudaHostAllocMapped));
@@ -405,10 +432,10 @@ static int build_tile_plan(ckt_graph *g, const std::vector<uint32_t> &off,
   *g->tile_error_host = 0u;
   CKT_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&g->tile_error), word, 0));
   g->tile_nodes = tile_nodes;
-  g->num_tiles = T;
-  g->tile_num_steps = (int64_t)steps.size();
+  g->num_tiles = hp.T;
+  g->tile_num_steps = (int64_t)hp.steps.size();
   g->tile_stream_steps = 0;
-  for (const uint4 &s : steps) g->tile_stream_steps += (s.z & kGhostStep) == 0u;
+  for (const uint4 &s : hp.steps) g->tile_stream_steps += (s.z & kGhostStep) == 0u;
   return CKT_OK;
 }
 

@@ -11,7 +11,11 @@ private nodes in place, shared/ghost nodes through folds flushed at group
 starts).  The result must equal, bit for bit, the sequential sum in CSR
 order that the gather form computes; the plan's layout invariants (16-byte
 blocks, step sizes, node ownership by warp, one run per node per step,
-lists opening with a head) are checked on the way.
+lists opening with a head) are checked on the way.  The whole-circuit plan
+is then replayed as the library uploads it: its packing list (each ghost
+slot once, sorted by source block and slot, with consistent block offsets
+and end flags) fills a ghost buffer whose padding stays NaN, every tile
+walks the concatenated steps from there, and the sums must match again.
 """
 import os
 import shutil
@@ -181,6 +185,94 @@ static int run(int P, int npp, int wpp, int nshared, double pct, uint64_t seed) 
   }
   for (int x = 0; x < N; x++)
     if (memcmp(&got[x], &ref[x], 4)) FAIL("node %d: %a against %a", x, got[x], ref[x]);
+
+  // The whole-circuit plan as the library uploads it: the packing list
+  // fills the ghost buffer (padding slots stay NaN and must never be read),
+  // and every tile replays from the concatenated steps and entries.
+  HostTilePlan hp;
+  if (make_tile_plan((uint32_t)N, W, off, ent, TN, hp)) FAIL("make_tile_plan failed");
+  if (hp.T != T || hp.tile_step.size() != T + 1 || hp.tile_step[T] != hp.steps.size())
+    FAIL("tile step table");
+  std::vector<float> ghost((size_t)hp.gslots, NAN);
+  std::vector<int> filled((size_t)hp.gslots, 0);
+  for (size_t k = 0; k < hp.glist.size(); k++) {
+    const uint2 g = hp.glist[k];
+    if (g.x >= (uint64_t)hp.gslots || filled[g.x]++) FAIL("ghost slot %u twice or out of range", g.x);
+    if ((g.y >> 1) >= (uint32_t)W) FAIL("ghost source wire out of range");
+    if (k > 0) {
+      const uint2 p = hp.glist[k - 1];
+      const uint32_t bp = (p.y >> 1) / kPackWires, bk = (g.y >> 1) / kPackWires;
+      if (bp > bk || (bp == bk && p.x >= g.x)) FAIL("packing list not sorted by (block, slot)");
+    }
+    ghost[g.x] = (g.y & 1u) ? I9[g.y >> 1] : I0[g.y >> 1];
+  }
+  if (hp.gblock.size() != hp.nblocks + 1 || hp.gblock[hp.nblocks] != hp.glist.size())
+    FAIL("packing block table size");
+  for (uint32_t b = 0; b < hp.nblocks; b++) {
+    const uint32_t f = hp.gblock[b] & kPackFirstMask, l = hp.gblock[b + 1] & kPackFirstMask;
+    if (f > l) FAIL("packing block %u runs backwards", b);
+    bool in = false, out = false;
+    for (uint32_t k = f; k < l; k++) {
+      if ((hp.glist[k].y >> 1) / kPackWires != b) FAIL("entry %u outside its block %u", k, b);
+      ((hp.glist[k].y & 1u) ? out : in) = true;
+    }
+    if (in != ((hp.gblock[b] & kPackHasIn) != 0) || out != ((hp.gblock[b] & kPackHasOut) != 0))
+      FAIL("packing block %u flags", b);
+  }
+  for (uint32_t t = 0; t < T; t++) {
+    const uint32_t x0 = t * TN, xe = std::min<uint32_t>(N, x0 + TN), nn = xe - x0;
+    std::vector<float> sacc(q0.begin() + x0, q0.begin() + xe), sfold(nn, 0.f);
+    for (uint32_t si = hp.tile_step[t]; si < hp.tile_step[t + 1]; si++) {
+      const uint4 st = hp.steps[si];
+      const uint16_t *hdr = reinterpret_cast<const uint16_t *>(hp.ent.data() + st.x);
+      const uint32_t total = hdr[kTileLanes];
+      const uint32_t *sent = hp.ent.data() + st.x + kStepHeaderWords;
+      std::vector<float> sval(2 * kChunkWires, NAN);
+      if ((st.z & kGhostStep) == 0u) {
+        for (uint32_t i = 0; i < kChunkWires && st.z * kChunkWires + i < (uint32_t)W; i++) {
+          sval[i] = I0[st.z * kChunkWires + i];
+          sval[kChunkWires + i] = I9[st.z * kChunkWires + i];
+        }
+      } else {
+        const uint32_t n0 = (((st.z >> kGhostCountBits) & kGhostCountMask) + 3u) & ~3u;
+        const uint32_t n1 = ((st.z & kGhostCountMask) + 3u) & ~3u;
+        if (st.w % 4 || st.w + n0 + n1 > hp.gslots) FAIL("ghost run of a step out of range");
+        for (uint32_t i = 0; i < n0; i++) sval[i] = ghost[st.w + i];
+        for (uint32_t i = 0; i < n1; i++) sval[kChunkWires + i] = ghost[st.w + n0 + i];
+      }
+      for (uint32_t l = 0; l < kTileLanes; l++) {
+        const uint32_t b = hdr[l], e = l + 1 < kTileLanes ? hdr[l + 1] : total;
+        uint32_t node = 0xffffffffu;
+        float acc = 0.f, fold = 0.f;
+        for (uint32_t p = b; p < e; p++) {
+          const uint32_t u = sent[p], end = (u & kTeEnd) ? 1u : 0u;
+          const float v = sval[end * kChunkWires + (u & (kChunkWires - 1))];
+          if (std::isnan(v)) FAIL("tile %u read an unfilled value", t);
+          if (u & kTeHead) {
+            if (node != 0xffffffffu) { sacc[node] = acc; sfold[node] = fold; }
+            node = (u >> kTeNodeShift) & (kTileNodesMax - 1);
+            acc = sacc[node];
+            fold = sfold[node];
+          }
+          const float c = end ? fmul(dt, v) : fmul(-dt, v);
+          if (u & kTePriv) {
+            acc = fadd(acc, c);
+          } else {
+            if (u & kTeFlush) { acc = fadd(acc, fold); fold = 0.f; }
+            fold = fadd(fold, c);
+          }
+        }
+        if (node != 0xffffffffu) { sacc[node] = acc; sfold[node] = fold; }
+      }
+    }
+    for (uint32_t i = 0; i < nn; i++) {
+      const uint32_t x = x0 + i;
+      float q = sacc[i];
+      if ((hp.mask[(size_t)t * (kTileNodesMax / 32) + i / 32] >> (i % 32)) & 1u) q = fadd(q, sfold[i]);
+      if (memcmp(&q, &ref[x], 4)) FAIL("whole plan, node %u: %a against %a", x, q, ref[x]);
+    }
+  }
+  printf("ghost %zu %d ", hp.glist.size(), hp.staged ? 1 : 0);
   return 0;
 }
 
@@ -194,9 +286,10 @@ int main() {
       {5, 20000, 3, 100, 0},        // nearly no wires, all cross
       {7, 3, 3000, 3, 60},          // hub nodes: runs longer than a step
       {1, 1, 8192, 0, 100},         // one node: 16384 entries
+      {16, 8192, 8192, 4096, 50},   // half the wires cross: staged packing
   };
   int rc = 0;
-  for (int i = 0; i < 8; i++) {
+  for (int i = 0; i < 9; i++) {
     const int r = run(cases[i].P, cases[i].npp, cases[i].wpp, cases[i].ns, cases[i].pct, 11 + i);
     printf("case %d: %s\n", i, r ? "FAILED" : "ok");
     rc |= r;
@@ -217,4 +310,10 @@ def test_tile_plan_replays_to_the_gather_bits(tmp_path):
                     "-lcudart", "-lpthread", f"-Wl,-rpath,{lib}"], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
-    assert out.stdout.count(": ok") == 8, out.stdout
+    assert out.stdout.count(": ok") == 9, out.stdout
+    # both packing forms and plans without ghost steps are among the cases
+    ghosts = [tuple(map(int, line.split("ghost ")[1].split()[:2]))
+              for line in out.stdout.splitlines() if "ghost " in line]
+    assert any(n > 0 and staged for n, staged in ghosts), out.stdout
+    assert any(n > 0 and not staged for n, staged in ghosts), out.stdout
+    assert any(n == 0 for n, _ in ghosts), out.stdout
