@@ -48,9 +48,10 @@ int ckt_check_recip_quotient(uint64_t seed, uint64_t count, int32_t divisor, int
 /* The quotient EXACT mode takes for the dividends outside that range
  * (scaled by a power of two into it; zeros and infinities times the
  * reciprocal) against __fdiv_rn on `count` pseudo-random pairs: dividends
- * huge up to FLT_MAX, tiny down to the divisor's bound (2^-118 for R, 2^-96
- * for C), in range, zero, infinite, NaN, or with a quotient within an ulp of
- * a rounding boundary or of overflowing.  Adds to counts[0] the mismatches,
+ * huge up to FLT_MAX, tiny down to the smallest subnormal (but not so tiny
+ * that the quotient may be subnormal: |a| >= 2^-125 |b|), in range, zero,
+ * infinite, NaN, or with a quotient within an ulp of a rounding boundary or
+ * of overflowing.  Adds to counts[0] the mismatches,
  * to counts[1] the pairs outside the guarded range, to counts[2] the pairs
  * drawn. */
 int ckt_check_wide_quotient(uint64_t seed, uint64_t count, int32_t divisor,

@@ -47,12 +47,12 @@
 //    normal, and when RN(a/b) overflows the scaled quotient is at least
 //    2^64 (2^128 - 2^103, the overflow threshold, scaled to the midpoint
 //    2^64 - 2^39, rounds up to the even 2^64), so multiplying back gives
-//    the same infinity.  A tiny |a| in [tiny, lo) is scaled by 2^80 into
-//    both ranges; multiplying back is exact while RN(a/b) is normal, which
-//    |a| >= tiny guarantees: tiny = 2^-126 times the largest divisor
-//    (kRTiny = 2^-118 for R, kCTiny = 2^-96 for C).  Zeros and infinities
-//    are a times RN(1/b), exact for them.  Nonzero dividends below tiny
-//    (whose quotients may be subnormal) are left to the divide routine.
+//    the same infinity.  A tiny nonzero |a| below lo, subnormals included,
+//    is scaled by 2^110 into [2^-39, 2^60), inside both ranges; multiplying
+//    back is exact while RN(a/b) is normal, which |a| >= 2^-125 |b|
+//    guarantees.  Zeros and infinities are a times RN(1/b), exact for them.
+//    Dividends whose quotient may be subnormal (subnormal_quot) are left to
+//    the divide routine.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -72,11 +72,9 @@ constexpr float kDtTiny = 0x1p-118f;
 // Eligible divisors and guarded dividend ranges of the corrected quotient.
 // R: |b| in [2^-8, 2^8], |a| in [2^-50, 2^100];
 // C and a general dt: |b| in [2^-30, 2^30], |a| in [2^-40, 2^90].
-// wide_quot is exact for every dividend but the nonzero ones below kRTiny /
-// kCTiny in magnitude.
+// wide_quot is exact for every dividend but those subnormal_quot flags.
 constexpr float kRMin = 0x1p-8f, kRMax = 0x1p8f, kRLo = 0x1p-50f, kRHi = 0x1p100f;
 constexpr float kCMin = 0x1p-30f, kCMax = 0x1p30f, kCLo = 0x1p-40f, kCHi = 0x1p90f;
-constexpr float kRTiny = 0x1p-118f, kCTiny = 0x1p-96f;
 
 __device__ __forceinline__ float dt_zh() { return __int_as_float((int)kDtZhBits); }
 __device__ __forceinline__ float dt_zl() { return __int_as_float((int)kDtZlBits); }
@@ -146,21 +144,32 @@ __device__ __forceinline__ bool tiny_nonzero(float a, float tiny) {
   return (m < tiny) & (m != 0.0f);
 }
 
-// RN(a/b) for any a but a nonzero one below the divisor's tiny bound:
-// the corrected quotient of a scaled into [lo, hi] (see above).
+// True when RN(a/b) may be subnormal: a nonzero |a| below 2^-125 |b|
+// (m * 2^125 is exact for the magnitudes compared; NaN: false).
+__device__ __forceinline__ bool subnormal_quot(float a, const Recip &k) {
+  const float m = fabsf(a);
+  return (m != 0.0f) & (__fmul_rn(m, 0x1p125f) < fabsf(k.nb));
+}
+__device__ __forceinline__ bool subnormal_quot2(float2 a, const Recip2 &k) {
+  const float2 m = __fmul2_rn(make_float2(fabsf(a.x), fabsf(a.y)), make_float2(0x1p125f, 0x1p125f));
+  return ((a.x != 0.0f) & (m.x < fabsf(k.nb.x))) | ((a.y != 0.0f) & (m.y < fabsf(k.nb.y)));
+}
+
+// RN(a/b) for any a that subnormal_quot does not flag: the corrected
+// quotient of a scaled into [lo, hi] (see above).
 __device__ __forceinline__ float wide_quot(float a, const Recip &k, float lo, float hi) {
   const float m = fabsf(a);
-  const float s = m > hi ? 0x1p-64f : (m < lo ? 0x1p80f : 1.0f);
-  const float u = m > hi ? 0x1p64f : (m < lo ? 0x1p-80f : 1.0f);
+  const float s = m > hi ? 0x1p-64f : (m < lo ? 0x1p110f : 1.0f);
+  const float u = m > hi ? 0x1p64f : (m < lo ? 0x1p-110f : 1.0f);
   const float q = __fmul_rn(recip_quot(__fmul_rn(a, s), k), u);
   return (m == 0.0f || m == __int_as_float(0x7f800000)) ? __fmul_rn(a, k.y) : q;
 }
 __device__ __forceinline__ float2 wide_quot2(float2 a, const Recip2 &k, float lo, float hi) {
   const float mx = fabsf(a.x), my = fabsf(a.y);
-  const float2 s = make_float2(mx > hi ? 0x1p-64f : (mx < lo ? 0x1p80f : 1.0f),
-                               my > hi ? 0x1p-64f : (my < lo ? 0x1p80f : 1.0f));
-  const float2 u = make_float2(mx > hi ? 0x1p64f : (mx < lo ? 0x1p-80f : 1.0f),
-                               my > hi ? 0x1p64f : (my < lo ? 0x1p-80f : 1.0f));
+  const float2 s = make_float2(mx > hi ? 0x1p-64f : (mx < lo ? 0x1p110f : 1.0f),
+                               my > hi ? 0x1p-64f : (my < lo ? 0x1p110f : 1.0f));
+  const float2 u = make_float2(mx > hi ? 0x1p64f : (mx < lo ? 0x1p-110f : 1.0f),
+                               my > hi ? 0x1p64f : (my < lo ? 0x1p-110f : 1.0f));
   float2 q = __fmul2_rn(recip_quot2(__fmul2_rn(a, s), k), u);
   const float2 z = __fmul2_rn(a, k.y);
   const float inf = __int_as_float(0x7f800000);

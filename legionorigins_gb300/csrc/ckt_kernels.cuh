@@ -227,8 +227,8 @@ struct DualExact {
     // infinities as a loop's state starts or blows up) takes wide_quot, and
     // the divide routine only for the rare dividends wide_quot does not
     // cover: with DTF a dt dividend below kDtTiny (whose split quotient may
-    // be off) or an R dividend below kRTiny, a C dividend below kCTiny;
-    // without DTF, phase 1 always.
+    // be off), an R or C dividend whose quotient may be subnormal; without
+    // DTF, phase 1 always.
     bool wide = false;  // phase 1 left the corrected quotient
     if (!bad) {
 #pragma unroll
@@ -239,7 +239,7 @@ struct DualExact {
 #pragma unroll
         for (int k = 0; k < 10; k++)
           rare |= tiny_nonzero(a1[k].x, kDtTiny) | tiny_nonzero(a1[k].y, kDtTiny) |
-                  tiny_nonzero(a2[k].x, kRTiny) | tiny_nonzero(a2[k].y, kRTiny);
+                  subnormal_quot2(a2[k], kR);
       }
       if (!rare) {
 #pragma unroll
@@ -276,7 +276,7 @@ struct DualExact {
       bool rare = false;
 #pragma unroll
       for (int k = 0; k < 9; k++)
-        rare |= tiny_nonzero(a3[k].x, kCTiny) | tiny_nonzero(a3[k].y, kCTiny);
+        rare |= subnormal_quot2(a3[k], kC);
       if (!rare) {
 #pragma unroll
         for (int k = 0; k < 9; k++) nv[k + 1] = __fadd2_rn(V0[k], wide_quot2(a3[k], kC, kCLo, kCHi));
@@ -388,7 +388,7 @@ struct SoloExact {
       if (DTF) {
 #pragma unroll
         for (int k = 0; k < 10; k++)
-          rare |= tiny_nonzero(a1[k], kDtTiny) | tiny_nonzero(a2[k], kRTiny);
+          rare |= tiny_nonzero(a1[k], kDtTiny) | subnormal_quot(a2[k], kR);
       }
       if (!rare) {
 #pragma unroll
@@ -418,7 +418,7 @@ struct SoloExact {
     } else {
       bool rare = false;
 #pragma unroll
-      for (int k = 0; k < 9; k++) rare |= tiny_nonzero(a3[k], kCTiny);
+      for (int k = 0; k < 9; k++) rare |= subnormal_quot(a3[k], kC);
       if (!rare) {
 #pragma unroll
         for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], wide_quot(a3[k], kC, kCLo, kCHi));

@@ -122,18 +122,16 @@ __global__ void __launch_bounds__(256)
 
 // wide_quot, the quotient of EXACT mode's phases that leave the guarded
 // range, against the divide routine: dividends of every class -- huge up to
-// FLT_MAX, tiny down to the divisor's bound, the guarded range, zeros,
+// FLT_MAX, tiny down to the smallest subnormal, the guarded range, zeros,
 // infinities, NaN, quotients within an ulp of a rounding boundary or of the
-// overflow threshold -- except the nonzero ones below the bound, which the
-// steppers leave to the divide routine.
+// overflow threshold -- except those whose quotient may be subnormal
+// (subnormal_quot), which the steppers leave to the divide routine.
 __global__ void __launch_bounds__(256)
     wide_quotient_check_kernel(uint64_t seed, uint64_t count, int32_t divisor,
                                unsigned long long *counts) {
   const int be0 = divisor == 0 ? -8 : -30, be1 = -be0 - 1;
   const float lo = divisor == 0 ? kRLo : kCLo, hi = divisor == 0 ? kRHi : kCHi;
-  const float tiny = divisor == 0 ? kRTiny : kCTiny;
-  const int tiny_e = divisor == 0 ? -118 : -96, lo_e = divisor == 0 ? -50 : -40,
-            hi_e = divisor == 0 ? 100 : 90;
+  const int lo_e = divisor == 0 ? -50 : -40, hi_e = divisor == 0 ? 100 : 90;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t rounds = (count + stride - 1) / stride;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -151,9 +149,11 @@ __global__ void __launch_bounds__(256)
       case 0:
         a = rand_float(h2, hi_e, 127);
         break;
-      case 1:
-        a = rand_float(h2, tiny_e, lo_e - 1);
+      case 1: {
+        const int e = -149 + (int)((uint32_t)(h2 >> 32) % (uint32_t)(lo_e + 149));
+        a = sgn * ldexpf(1.0f + (float)(h2 & 0x7fffffu) * 0x1p-23f, e);
         break;
+      }
       case 2: {
         const float sp[8] = {0.0f, __uint_as_float(0x7f800000u), __uint_as_float(0x7fc00000u),
                              fmax, lo, hi, __uint_as_float(__float_as_uint(hi) + 1u),
@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(256)
         a = rand_float(h2, -126, 127);
         break;
     }
-    if (tiny_nonzero(a, tiny)) continue;
     const Recip k = make_recip(b);
+    if (subnormal_quot(a, k)) continue;
     bad += !same_float(wide_quot(a, k, lo, hi), __fdiv_rn(a, b));
     out += outside(a, lo, hi);
     drawn++;

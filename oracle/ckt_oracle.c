@@ -725,18 +725,19 @@ void ocl_split_quotient_check(uint64_t lo, uint64_t hi, float dt, float zh, floa
 /* The R and C quotients of calc_new_currents (apps/circuit/circuit.cc:
  * 394-400, circuit_gpu.cu:123-128) as the GPU's EXACT mode evaluates a
  * dividend outside the corrected quotient's guarded range [lo, hi]: scaled
- * by 2^-64 (above hi) or 2^80 (below lo) into it, divided by the corrected
+ * by 2^-64 (above hi) or 2^110 (below lo) into it, divided by the corrected
  * quotient (q0 = fmaf(a, y, a*yl), r = fmaf(q0, -b, a), q = fmaf(r, y, q0)
  * with y = RN(1/b), yl = RN(1/b - y)), and scaled back; zeros and
  * infinities as a*y.  Draws `n` (dividend, divisor) pairs from seed --
  * divisors in [2^-8, 2^8) (divisor 0, R) or [2^-30, 2^30) (1, C), dividends
- * from every class: huge up to FLT_MAX, tiny down to the bound `tiny`, the
- * guarded range, zeros, infinities, NaN, and values whose quotient lies
- * within an ulp of a rounding boundary or of the overflow threshold -- and
- * counts the pairs whose result differs from the IEEE quotient a/b
- * (`bad`; equal means equal bits, or both NaN), the pairs taken outside
- * [lo, hi] (`outside`) and all pairs drawn.  Nonzero dividends below
- * `tiny` are not drawn: the GPU leaves them to its divide routine. */
+ * from every class: huge up to FLT_MAX, tiny down to the smallest
+ * subnormal, the guarded range, zeros, infinities, NaN, and values whose
+ * quotient lies within an ulp of a rounding boundary or of the overflow
+ * threshold -- and counts the pairs whose result differs from the IEEE
+ * quotient a/b (`bad`; equal means equal bits, or both NaN), the pairs taken
+ * outside [lo, hi] (`outside`) and all pairs drawn.  Pairs whose quotient
+ * may be subnormal (a nonzero |a| below 2^-125 |b|) are not drawn: the GPU
+ * leaves them to its divide routine. */
 static uint64_t wq_mix(uint64_t x)
 {
   x ^= x >> 30;
@@ -778,8 +779,8 @@ static float wq_recip_quot(float a, float y, float yl, float nb)
 static float wq_wide_quot(float a, float y, float yl, float nb, float lo, float hi)
 {
   const float m = fabsf(a);
-  const float s = m > hi ? 0x1p-64f : (m < lo ? 0x1p80f : 1.0f);
-  const float u = m > hi ? 0x1p64f : (m < lo ? 0x1p-80f : 1.0f);
+  const float s = m > hi ? 0x1p-64f : (m < lo ? 0x1p110f : 1.0f);
+  const float u = m > hi ? 0x1p64f : (m < lo ? 0x1p-110f : 1.0f);
   const float q = wq_recip_quot(a * s, y, yl, nb) * u;
   return (m == 0.0f || isinf(m)) ? a * y : q;
 }
@@ -789,8 +790,7 @@ void ocl_wide_quotient_check(uint64_t seed, uint64_t n, int divisor, uint64_t *b
 {
   const int be0 = divisor == 0 ? -8 : -30, be1 = -be0 - 1;
   const float lo = divisor == 0 ? 0x1p-50f : 0x1p-40f, hi = divisor == 0 ? 0x1p100f : 0x1p90f;
-  const int tiny_e = divisor == 0 ? -118 : -96, lo_e = divisor == 0 ? -50 : -40,
-            hi_e = divisor == 0 ? 100 : 90;
+  const int lo_e = divisor == 0 ? -50 : -40, hi_e = divisor == 0 ? 100 : 90;
   uint64_t nbad = 0, nout = 0, nd = 0;
   for (uint64_t i = 0; i < n; i++) {
     const uint64_t h1 = wq_mix(seed * 0x9e3779b97f4a7c15ull + 2 * i + 1);
@@ -802,9 +802,11 @@ void ocl_wide_quotient_check(uint64_t seed, uint64_t n, int divisor, uint64_t *b
       case 0:  /* huge */
         a = wq_rand(h2, hi_e, 127);
         break;
-      case 1:  /* tiny, down to the bound */
-        a = wq_rand(h2, tiny_e, lo_e - 1);
+      case 1: {  /* tiny, subnormals included */
+        const int e = -149 + (int)((uint32_t)(h2 >> 32) % (uint32_t)(lo_e + 149));
+        a = sgn * ldexpf(1.0f + (float)(h2 & 0x7fffffu) * 0x1p-23f, e);
         break;
+      }
       case 2: {  /* special values and the range edges */
         const float sp[8] = {0.0f, INFINITY, NAN, FLT_MAX, lo, hi, wq_bits(wq_u(hi) + 1u),
                              wq_bits(wq_u(lo) - 1u)};
@@ -830,7 +832,7 @@ void ocl_wide_quotient_check(uint64_t seed, uint64_t n, int divisor, uint64_t *b
         a = wq_rand(h2, -126, 127);
         break;
     }
-    if (isfinite(a) && a != 0.0f && fabsf(a) < ldexpf(1.0f, tiny_e)) continue;
+    if (a != 0.0f && fabsf(a) * 0x1p125f < fabsf(b)) continue;
     nd++;
     const float y = 1.0f / b, yl = fmaf(-b, y, 1.0f) / b;
     const float got = wq_wide_quot(a, y, yl, -b, lo, hi), want = a / b;

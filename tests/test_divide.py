@@ -60,8 +60,9 @@ def test_wide_quotient_equals_ieee_division(oracle):
     """EXACT mode's quotient by R and C for dividends outside the corrected
     quotient's guarded range -- scaled by a power of two into it, zeros and
     infinities as a times RN(1/b) -- restated in C with fmaf: equal to IEEE
-    a/b on every pair drawn (huge, tiny down to the divisor's bound, zeros,
-    infinities, NaN, near rounding boundaries and near overflow).  The GPU
+    a/b on every pair drawn (huge, tiny down to the smallest subnormal as
+    long as the quotient stays normal, zeros, infinities, NaN, near rounding
+    boundaries and near overflow).  The GPU
     test (tests/test_gpu_divide.py) repeats it against __fdiv_rn."""
     for divisor in (0, 1):
         bad, outside, drawn = oracle.wide_quotient_check(11 + divisor, 1 << 22, divisor)

@@ -51,8 +51,8 @@ def test_corrected_quotient_random_pairs(cuda, ckt, divisor, near_ties):
 def test_wide_quotient_random_pairs(cuda, ckt, divisor):
     """The quotient of the phases that leave the guarded range (the state's
     zeros at the start of a loop, huge values and infinities as it blows
-    up): every class of dividend, the nonzero ones below the divisor's tiny
-    bound excepted, equals __fdiv_rn."""
+    up): every class of dividend, those whose quotient may be subnormal
+    excepted, equals __fdiv_rn."""
     c = counts(cuda, 3)
     n = 1 << 30
     ckt.check(ckt.tools().ckt_check_wide_quotient(4321 + divisor, n, divisor, c.data_ptr(), None))
