@@ -60,11 +60,32 @@ WireArrays wire_arrays(const ckt_wires &w) {
   return a;
 }
 
+// SMs of the calling thread's current device (looked up once per device).
+static int device_sms() {
+  static thread_local int dev_cached = -1, sms = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (dev != dev_cached) {
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 0;
+    dev_cached = dev;
+  }
+  return sms;
+}
+
 template <int M, int I>
 static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const float *vp,
                          const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
   const WireArrays a = wire_arrays(w);
   const NodeVolts v = {vp, vs, vg};
+  // EXACT with at most two warps per SM scheduler: one wire per thread in
+  // one-warp blocks, spread over every SM, runs each step several times
+  // faster than the paired kernel on the few SMs its blocks would occupy
+  // (same bits: the scalar and paired steppers round every operation alike).
+  const int sms = M == CKT_MODE_EXACT ? device_sms() : 0;
+  if (M == CKT_MODE_EXACT && sms > 0 && n <= 256u * (uint32_t)sms) {
+    cnc_kernel<M, I><<<grid_for(n, 32), 32, 0, s>>>(first, n, a, v, p->steps, p->dt);
+    return;
+  }
   if constexpr (M == CKT_MODE_FAST || M == CKT_MODE_EXACT)  // two wires per thread, paired
     cnc_pair_kernel<M, I><<<grid_for(n, 2 * kPairBlock), kPairBlock, 0, s>>>(first, n, a, v,
                                                                              p->steps, p->dt);
