@@ -311,6 +311,9 @@ struct DualExact {
 #pragma unroll
     for (int k = 0; k < 9; k++) nv[k + 1] = __fadd2_rn(V0[k], recip_quot2(a3[k], kC));
   }
+  static __device__ __forceinline__ bool first_nan(const float2 (&ni)[10]) {
+    return ni[0].x != ni[0].x;
+  }
   static __device__ __forceinline__ bool all_nan(const float2 (&ni)[10], const float2 (&nv)[11]) {
     bool nan = true;
 #pragma unroll
@@ -328,17 +331,16 @@ struct DualExact {
 // step_all_nan -- every operation of every step still computed, the same
 // bits.
 constexpr int kNanCheckSteps = 16;
-template <bool DTF>
-__device__ __forceinline__ void exact_steps(const DualExact<DTF> &pk, int steps,
-                                            float2 (&ni)[10], float2 (&nv)[11],
-                                            const float2 (&nI0)[10], const float2 (&V0)[9]) {
+template <typename Stepper, typename F>
+__device__ __forceinline__ void exact_steps(const Stepper &pk, int steps, F (&ni)[10], F (&nv)[11],
+                                            const F (&nI0)[10], const F (&V0)[9]) {
   int j = 0;
 #pragma unroll 1
   while (j < steps) {
     // The full test only once the first current is NaN (one compare on a
     // finite state); the switch only when every thread of the warp can take
     // it, so that a warp never runs the two loops one after the other.
-    const bool mine = ni[0].x != ni[0].x && DualExact<DTF>::all_nan(ni, nv);
+    const bool mine = Stepper::first_nan(ni) && Stepper::all_nan(ni, nv);
     if (__all_sync(__activemask(), mine)) break;
     const int n = min(kNanCheckSteps, steps - j);
 #pragma unroll 1
@@ -428,6 +430,36 @@ struct SoloExact {
         for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], __fdiv_rn(a3[k], C));
       }
     }
+  }
+  // step() for a state whose 10 currents and 9 wire voltages are all NaN:
+  // the same operations without the compares and the branches (see
+  // DualExact::step_all_nan).
+  __device__ __forceinline__ void step_all_nan(float (&ni)[10], float (&nv)[11],
+                                               const float (&I0)[10],
+                                               const float (&V0)[9]) const {
+    float a2[10];
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+      const float a1 = __fmul_rn(L, __fsub_rn(ni[k], I0[k]));
+      const float q1 = DTF ? dt_quot(a1) : recip_quot(a1, kdt);
+      a2[k] = __fsub_rn(__fsub_rn(nv[k + 1], nv[k]), q1);
+    }
+#pragma unroll
+    for (int k = 0; k < 10; k++) ni[k] = recip_quot(a2[k], kR);
+    float a3[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) a3[k] = __fmul_rn(dt, __fsub_rn(ni[k], ni[k + 1]));
+#pragma unroll
+    for (int k = 0; k < 9; k++) nv[k + 1] = __fadd_rn(V0[k], recip_quot(a3[k], kC));
+  }
+  static __device__ __forceinline__ bool first_nan(const float (&ni)[10]) { return ni[0] != ni[0]; }
+  static __device__ __forceinline__ bool all_nan(const float (&ni)[10], const float (&nv)[11]) {
+    bool nan = true;
+#pragma unroll
+    for (int k = 0; k < 10; k++) nan &= ni[k] != ni[k];
+#pragma unroll
+    for (int k = 1; k < 10; k++) nan &= nv[k] != nv[k];
+    return nan;
   }
 };
 
@@ -532,13 +564,11 @@ __device__ __forceinline__ void cnc_wire(int64_t w, const WireArrays &a, const N
   } else if (MODE == CKT_MODE_EXACT && __float_as_uint(dt) == kDtBits &&
              SoloExact<true>::eligible(a.R[w], a.C[w], dt)) {
     const SoloExact<true> ws(a.L[w], a.R[w], a.C[w], dt);
-#pragma unroll 1
-    for (int j = 0; j < steps; j++) ws.step(ni, nv, I0, V0);
+    exact_steps(ws, steps, ni, nv, I0, V0);
   } else if (MODE == CKT_MODE_EXACT && __float_as_uint(dt) != kDtBits &&
              SoloExact<false>::eligible(a.R[w], a.C[w], dt)) {
     const SoloExact<false> ws(a.L[w], a.R[w], a.C[w], dt);
-#pragma unroll 1
-    for (int j = 0; j < steps; j++) ws.step(ni, nv, I0, V0);
+    exact_steps(ws, steps, ni, nv, I0, V0);
   } else {
     static_assert(MODE == CKT_MODE_EXACT || MODE == CKT_MODE_EXACT_DIVIDE, "unknown mode");
     const DivideStep ws(a.L[w], a.R[w], a.C[w], dt);

@@ -77,12 +77,12 @@ static void launch_cnc_t(uint32_t first, uint32_t n, const ckt_wires &w, const f
                          const float *vs, const float *vg, const ckt_params *p, cudaStream_t s) {
   const WireArrays a = wire_arrays(w);
   const NodeVolts v = {vp, vs, vg};
-  // EXACT with at most two warps per SM scheduler: one wire per thread in
+  // EXACT with at most three warps per SM scheduler: one wire per thread in
   // one-warp blocks, spread over every SM, runs each step several times
   // faster than the paired kernel on the few SMs its blocks would occupy
   // (same bits: the scalar and paired steppers round every operation alike).
   const int sms = M == CKT_MODE_EXACT ? device_sms() : 0;
-  if (M == CKT_MODE_EXACT && sms > 0 && n <= 256u * (uint32_t)sms) {
+  if (M == CKT_MODE_EXACT && sms > 0 && n <= 384u * (uint32_t)sms) {
     cnc_kernel<M, I><<<grid_for(n, 32), 32, 0, s>>>(first, n, a, v, p->steps, p->dt);
     return;
   }
